@@ -1,0 +1,330 @@
+"""Benchmark of the Johansen null-eigenspectra hot path on GB300.
+
+Workload (the headline configuration): dim 12, T = 10,000 steps, models 0-4.
+One step = one batch of R runs for each of the five models, each model a
+separate C-ABI request (seeds 1..R, counter-based Philox increments generated
+in-kernel), through the mixed-precision path (split-TF32 tensor-core Grams,
+FP32 chunks, FP64 merge and FP64 Cholesky + tridiagonal QL).
+
+  value   runs/s with results left in device memory (jne_eigs_seeded_device)
+  e2e     runs/s through jne_eigs_seeded: eigenvalues copied to host memory
+  fp64_plain  runs/s of the plain FP64 fused kernel on the same workload
+  mixed_error max relative max-eig / trace error of mixed vs FP64 on identical seeds
+
+`--impl reference` times the CPU restatement of the reference algorithm (the
+reference crate is Rust and cannot be built here) on all host cores.
+Multi-GPU (torchrun): replicas over disjoint seed ranges, no collective on the
+data path; only the timing barrier and a max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIM, STEPS, MODELS = 12, 10_000, (0, 1, 2, 3, 4)
+METRIC = "runs/s at dim12 T=10k, FP64 vs mixed-precision at stated error; p50/p99 latency"
+UNIT = "runs/s"
+
+
+def k_of(model: int) -> int:
+    return DIM + 1 if model in (1, 3) else DIM
+
+
+def canonical_flops(model: int) -> float:
+    """W = T k (k + 1 + 2 dim): S11 (symmetric) + S10 multiply-adds, 2 flops each."""
+    k = k_of(model)
+    return STEPS * k * (k + 1 + 2 * DIM)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def cpu_sample(oracle, runs_per_model: int, threads: int):
+    """Oracle (dense restatement) on `threads` host threads; returns runs/s."""
+    t0 = time.perf_counter()
+    for m in MODELS:
+        oracle.c_eigs_seeded(m, DIM, STEPS, 1, runs_per_model, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return len(MODELS) * runs_per_model / dt, dt
+
+
+def run_reference(args, rank: int, world: int) -> None:
+    if rank != 0:
+        return
+    import __graft_entry__ as entry
+
+    oracle = entry.load_oracle()
+    threads = os.cpu_count() or 1
+    per_model = args.cpu_runs or max(threads, 4 * threads)
+    for _ in range(args.warmup):
+        cpu_sample(oracle, max(threads, per_model // 4), threads)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_sample(oracle, per_model, threads)
+        times.append(dt)
+    total = sum(times)
+    value = len(MODELS) * per_model * args.steps / total
+    sample = f"{per_model} runs x 5 models per step (seeds 1..{per_model}), dim {DIM}, T {STEPS}"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (counter-based Philox normals)",
+        "config": {"workload": f"dim {DIM}, T {STEPS}, models 0-4, CPU restatement of the reference algorithm",
+                   "runs_per_model_per_step": per_model},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_gpu(args, rank: int, world: int) -> None:
+    import torch
+
+    import __graft_entry__ as entry
+
+    jne = entry.load_package()
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    eng = jne.Engine(local, chunk=args.chunk)
+    R = args.runs
+    seed0 = 1 + rank * R  # disjoint seed ranges per replica
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    outs = {m: torch.empty((R, k_of(m)), dtype=torch.float64, device="cuda") for m in MODELS}
+
+    def step_device(prec, lat=None):
+        for m in MODELS:
+            if lat is not None:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            eng.eigs_seeded_device(m, DIM, STEPS, seed0, R, outs[m].data_ptr(), precision=prec, stream=sptr)
+            if lat is not None:
+                e1 = torch.cuda.Event(enable_timing=True)
+                e1.record(stream)
+                lat.append((e0, e1))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- mixed precision, device-resident outputs (value) ----
+    for _ in range(args.warmup):
+        step_device(jne.PREC_MIXED)
+    barrier()
+    lat = []
+    eng.profile(True)  # per-kernel CUDA events on the launching stream
+    eng.profile_read(reset=True)
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step_device(jne.PREC_MIXED, lat)
+        ev1.record(stream)
+        barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    prof = eng.profile_read(reset=True)
+    eng.profile(False)
+    runs_per_step = R * len(MODELS) * world
+    value = runs_per_step * args.steps / (ms * 1e-3)
+    lat_ms = sorted(a.elapsed_time(b) for a, b in lat)
+    p50 = float(np.percentile(lat_ms, 50))
+    p99 = float(np.percentile(lat_ms, 99))
+
+    # ---- end to end through the host-memory C call (e2e) ----
+    host = {m: np.empty((R, k_of(m))) for m in MODELS}
+
+    def step_host():
+        for m in MODELS:
+            host[m] = eng.eigs_seeded(m, DIM, STEPS, seed0, R, precision=jne.PREC_MIXED)
+
+    step_host()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = runs_per_step * args.steps / e2e_s
+    d2h = sum(R * k_of(m) * 8 for m in MODELS)
+
+    # ---- plain FP64 fused kernel on the same workload (fewer runs) ----
+    Rf = args.fp64_runs
+    for m in MODELS:
+        eng.eigs_seeded_device(m, DIM, STEPS, seed0, Rf, outs[m].data_ptr(), precision=jne.PREC_FP64, stream=sptr)
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for m in MODELS:
+        eng.eigs_seeded_device(m, DIM, STEPS, seed0, Rf, outs[m].data_ptr(), precision=jne.PREC_FP64, stream=sptr)
+    f1.record(stream)
+    barrier()
+    fp64_ms = max_over_ranks(f0.elapsed_time(f1))
+    fp64_value = Rf * len(MODELS) * world / (fp64_ms * 1e-3)
+
+    # ---- accuracy of mixed vs FP64 on identical seeds (subset) ----
+    err = {}
+    ns = min(args.err_runs, R)
+    for m in MODELS:
+        f = eng.eigs_seeded(m, DIM, STEPS, seed0, ns, precision=jne.PREC_FP64)
+        x = eng.eigs_seeded(m, DIM, STEPS, seed0, ns, precision=jne.PREC_MIXED)
+        err[str(m)] = {"maxeig": float(np.max(np.abs(x[:, 0] - f[:, 0]) / f[:, 0])),
+                       "trace": float(np.max(np.abs(x.sum(1) - f.sum(1)) / f.sum(1)))}
+
+    # ---- dominant kernel: mixed accumulation, from the timed region's events ----
+    acc_ms, acc_n = prof["accum_mixed"]
+    fin_ms, fin_n = prof["finalize"]
+    kern = {"accum_mixed": {"launches": acc_n, "total_ms": acc_ms, "mean_ms": acc_ms / max(acc_n, 1)},
+            "finalize": {"launches": fin_n, "total_ms": fin_ms, "mean_ms": fin_ms / max(fin_n, 1)},
+            "share_accum": acc_ms / max(acc_ms + fin_ms, 1e-9)}
+    mean_acc_ms = acc_ms / max(acc_n, 1)
+    peaks = measured_peaks()
+    bf16 = peaks.get("bf16_tflops")
+    W = sum(canonical_flops(m) for m in MODELS) / len(MODELS)
+    achieved = W * R / (mean_acc_ms * 1e-3) / 1e12
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+            "frac": (achieved / bf16) if bf16 else None, "traffic": args.traffic,
+            "kernel": "k_accum_mixed<12,false>", "peak_source": "measured bf16_tflops (burst)" if bf16 else "none",
+            "flops_per_run": W}
+    normals_rate = DIM * STEPS * R / (mean_acc_ms * 1e-3)
+    issue = {"normals_per_s": normals_rate, "peak_normals_per_s": args.rng_peak,
+             "frac": normals_rate / args.rng_peak,
+             "note": "Philox4x32-10 + Box-Muller rate measured by a standalone throughput kernel on GB300"}
+
+    cpu = None
+    if rank == 0 and args.cpu_runs != 0:
+        oracle = entry.load_oracle()
+        threads = os.cpu_count() or 1
+        per = args.cpu_runs or 4 * threads
+        v, dt = cpu_sample(oracle, per, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{per} runs x 5 models (seeds 1..{per}), dim {DIM}, T {STEPS}, {dt:.1f} s wall"}
+
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "tf32x3-split/f32/f64", "data": "synthetic (in-kernel Philox normals)",
+            "config": {"workload": f"dim {DIM}, T {STEPS}, models 0-4, {R} runs per model per step "
+                                   f"(one request per model), mixed precision",
+                       "runs_per_model_per_step": R, "chunk": args.chunk,
+                       "l2": "working set larger than L2: moment records of a 5-model step are "
+                             f"{R * 294 * 8 * 5 / 1e9:.2f} GB; no inputs (increments generated in-kernel)",
+                       "parallelism": f"replicas x{world} over disjoint seed ranges"},
+            "latency_ms": {"per_request_p50": p50, "per_request_p99": p99,
+                           "request": f"{R} runs of one model"},
+            "fp64_plain": {"value": fp64_value, "unit": UNIT, "runs_per_model": Rf,
+                           "mixed_speedup": value / fp64_value},
+            "mixed_error": {"vs": "plain FP64 kernel, identical seeds", "runs_per_model": ns, "per_model": err},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
+            "gpu_launches": acc_n + fin_n,
+            "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--runs", type=int, default=200_000, help="runs per model per step")
+    ap.add_argument("--fp64-runs", type=int, default=20_000)
+    ap.add_argument("--err-runs", type=int, default=2_000)
+    ap.add_argument("--cpu-runs", type=int, default=None, help="CPU sample runs per model (0 = skip)")
+    ap.add_argument("--chunk", type=int, default=256)
+    ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per accumulation launch")
+    ap.add_argument("--rng-peak", type=float, default=1.016e12, help="measured Philox+Box-Muller normals/s")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

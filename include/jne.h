@@ -1,0 +1,120 @@
+/*
+ * jne.h -- C ABI of the GB300 engine for the Johansen null-eigenspectra
+ * Monte Carlo path (Kuan-Lun/johansen-null-eigenspectra).
+ *
+ * Plain C types only.  Every function returns a status code (JNE_OK = 0) and
+ * writes results into caller-owned buffers.  A context is used from one host
+ * thread at a time.  Eigenvalues are reported as the reference reports them:
+ * |alpha|/beta of the pencil (S10'S10, S11), sorted descending, k per run with
+ * k = dim + 1 for models 1 and 3 and k = dim otherwise.
+ *
+ * Reference interfaces replaced (paths within the reference crate):
+ *   jne_eigen_count            src/data_storage/thread_manager.rs:40-44
+ *   jne_eigs_from_increments   src/johansen_statistics.rs:24-85 (from the
+ *                              increment matrix rather than a seed)
+ *   jne_eigs_seeded(_device)   the per-seed calculate_eigenvalues calls of
+ *                              src/data_storage/parallel_compute.rs:14-41
+ *                              (johansen_statistics.rs:59-85 for seeds
+ *                              seed_first .. seed_first + n_runs - 1)
+ *   jne_eigs_seeded_models     the same, for several models of one
+ *                              (dim, steps) pair in one pass (the CLI loop over
+ *                              models, src/main.rs:109-114)
+ *   jne_export_increments      src/rng_matrix.rs:57-141 (the path itself)
+ *   jne_dat_*                  src/data_storage/{writer,reader,uleb128}.rs
+ *   jne_simulation_*           src/data_storage/simulation.rs:25-122 and
+ *                              parallel_compute.rs:150-232
+ *   jne_percentiles            src/simulation_analyzers.rs:4-81
+ */
+#ifndef JNE_H
+#define JNE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define JNE_OK 0
+#define JNE_ERR_ARG 1     /* bad argument (model, dim, steps, sizes, null pointers) */
+#define JNE_ERR_BUDGET 2  /* request does not fit the context's device-memory budget */
+#define JNE_ERR_CUDA 3    /* CUDA runtime error (no device, launch failure, ...) */
+#define JNE_ERR_TIMEOUT 4 /* a bounded device wait ran out */
+#define JNE_ERR_NUMERIC 5 /* S11 not positive definite for some run (NaN written) */
+#define JNE_ERR_IO 6      /* file system error */
+#define JNE_ERR_FORMAT 7  /* not an EIGENVALS_V6 file, or inconsistent records */
+
+/* arithmetic of the Gram contraction */
+#define JNE_PREC_FP64 0  /* plain FP64 fused kernel */
+#define JNE_PREC_MIXED 1 /* split-TF32 tensor-core Grams, FP32 chunks, FP64 merge + solve */
+
+#define JNE_MAX_DIM 12
+#define JNE_DEFAULT_BASE_SEED 0x4A4F48ull
+
+typedef struct jne_context jne_context;
+
+/* library version (major * 10000 + minor * 100 + patch) */
+int jne_version(void);
+
+/* number of eigenvalues per run, or -1 for a bad (model, dim) */
+int jne_eigen_count(int model, int dim);
+
+/* Opens a context on CUDA device `device`; device allocations of the context
+ * never exceed mem_budget_bytes (0 = 40 GiB). */
+int jne_open(int device, unsigned long long mem_budget_bytes, jne_context** out);
+void jne_close(jne_context* ctx);
+
+/* message of the last failed call on ctx (never null) */
+const char* jne_last_error(const jne_context* ctx);
+
+/* steps per FP32 chunk of the mixed kernel (multiple of 32; default 256) */
+int jne_set_chunk(jne_context* ctx, int chunk);
+
+/* Eigenvalues of n_runs runs from explicit increments.  dB holds n_runs
+ * consecutive dim x steps column-major matrices (dB[:, i] = B_{i+1} - B_i,
+ * B_0 = 0), host memory; out receives n_runs x k values (host). */
+int jne_eigs_from_increments(jne_context* ctx, int model, int dim, int steps, const double* dB, int n_runs,
+                             int precision, double* out);
+
+/* Eigenvalues of runs with seeds seed_first .. seed_first + n_runs - 1 drawn
+ * from the counter-based stream (base_seed, dim); out is host memory. */
+int jne_eigs_seeded(jne_context* ctx, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
+                    int64_t n_runs, int precision, double* out);
+
+/* As jne_eigs_seeded, with out in device memory, enqueued on `stream` (a
+ * cudaStream_t; null = the context's stream) and synchronised before return. */
+int jne_eigs_seeded_device(jne_context* ctx, int model, int dim, int steps, uint64_t base_seed,
+                           uint32_t seed_first, int64_t n_runs, int precision, double* out_device, void* stream);
+
+/* Several models of one (dim, steps) pair from one pass over the paths (the
+ * path of a seed does not depend on the model).  models[m] lists n_models
+ * model ids; outs[m] receives n_runs x k(models[m], dim) values (host). */
+int jne_eigs_seeded_models(jne_context* ctx, const int* models, int n_models, int dim, int steps,
+                           uint64_t base_seed, uint32_t seed_first, int64_t n_runs, int precision,
+                           double* const* outs);
+
+/* Per-kernel timing: when enabled, every kernel launch of ctx is bracketed by
+ * CUDA events on its launching stream.  jne_profile_read returns the summed
+ * device milliseconds and launch counts per kernel kind (index JNE_KERNEL_*),
+ * and resets them when `reset` is non-zero. */
+#define JNE_KERNEL_ACCUM_FP64 0
+#define JNE_KERNEL_ACCUM_MIXED 1
+#define JNE_KERNEL_FINALIZE 2
+#define JNE_KERNEL_EXPORT 3
+#define JNE_KERNEL_KINDS 4
+int jne_profile(jne_context* ctx, int enable);
+int jne_profile_read(jne_context* ctx, double* ms, long long* launches, int reset);
+
+/* The increments the seeded path draws for these runs, scaled by sqrt(1/steps):
+ * dB_out receives n_runs consecutive dim x steps column-major matrices (may be
+ * null); words_out receives the raw Philox words, n_runs x steps x
+ * ceil(dim/4) x 4 (may be null).  Host memory. */
+int jne_export_increments(jne_context* ctx, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
+                          int n_runs, double* dB_out, uint32_t* words_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JNE_H */

@@ -1,0 +1,228 @@
+"""GB300 engine for the Johansen null-eigenspectra Monte Carlo path.
+
+Python host mirror of the reference crate's public API (src/lib.rs:10-11):
+``JohansenModel`` and ``EigenvalueSimulation`` keep the reference's names,
+argument meaning and error behaviour, and every computation goes through the
+C ABI of ``libjne_gb300.so`` (include/jne.h) -- hand-written sm_103a kernels.
+There is no CPU fallback: a missing library or device raises.
+
+The directory name contains hyphens, so load this package with
+``load_package()`` from ``__graft_entry__`` (or importlib) rather than import.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libjne_gb300.so")
+
+JNE_OK, JNE_ERR_ARG, JNE_ERR_BUDGET, JNE_ERR_CUDA, JNE_ERR_TIMEOUT, JNE_ERR_NUMERIC, JNE_ERR_IO, JNE_ERR_FORMAT = range(8)
+PREC_FP64, PREC_MIXED = 0, 1
+DEFAULT_BASE_SEED = 0x4A4F48
+MAX_DIM = 12
+
+# every symbol include/jne.h declares (checked by the CPU test suite)
+EXPORTS = (
+    "jne_version", "jne_eigen_count", "jne_open", "jne_close", "jne_last_error", "jne_set_chunk",
+    "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
+    "jne_export_increments", "jne_profile", "jne_profile_read",
+)
+KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
+
+
+class JneError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[jne status {code}] {msg}")
+        self.code = code
+
+
+class JohansenModel(enum.IntEnum):
+    """The five Johansen models (johansen_models.rs:6-26)."""
+
+    NoInterceptNoTrend = 0
+    InterceptNoTrendWithInterceptInCoint = 1
+    InterceptNoTrendUnrestrictedIntercept = 2
+    InterceptTrendUnrestrictedInterceptRestrictedTrend = 3
+    InterceptTrendUnrestrictedBoth = 4
+
+    def to_number(self) -> int:
+        return int(self)
+
+    @classmethod
+    def from_number(cls, n: int) -> Optional["JohansenModel"]:
+        return cls(n) if 0 <= n <= 4 else None
+
+    def description(self) -> str:  # johansen_models.rs:54-70
+        return _DESCRIPTIONS[int(self)]
+
+    def has_intercept(self) -> bool:
+        return self != JohansenModel.NoInterceptNoTrend
+
+    def has_trend(self) -> bool:
+        return self in (JohansenModel.InterceptTrendUnrestrictedInterceptRestrictedTrend,
+                        JohansenModel.InterceptTrendUnrestrictedBoth)
+
+    def intercept_fully_explained_by_cointegration(self) -> bool:
+        return self == JohansenModel.InterceptNoTrendWithInterceptInCoint
+
+    def trend_fully_explained_by_cointegration(self) -> bool:
+        return self == JohansenModel.InterceptTrendUnrestrictedInterceptRestrictedTrend
+
+    @classmethod
+    def all_models(cls) -> List["JohansenModel"]:
+        return [cls(i) for i in range(5)]
+
+    @classmethod
+    def default(cls) -> "JohansenModel":  # johansen_models.rs:130-135
+        return cls.InterceptNoTrendUnrestrictedIntercept
+
+    def __str__(self) -> str:  # johansen_models.rs:137-141
+        return f"Model {int(self)}: {self.description()}"
+
+
+_DESCRIPTIONS = (
+    "No intercept, no trend",
+    "Intercept, no trend, intercept in cointegration",
+    "Intercept, no trend, intercept not fully explained by cointegration",
+    "Intercept, trend, trend in cointegration",
+    "Intercept, trend, intercept and trend not fully explained by cointegration",
+)
+
+
+def eigen_count(model: int, dim: int) -> int:
+    """thread_manager.rs:40-44."""
+    return dim + 1 if int(model) in (1, 3) else dim
+
+
+# --------------------------------------------------------------------------
+# ctypes binding
+# --------------------------------------------------------------------------
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libjne_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing: run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        c_int, c_u32, c_u64, c_i64, c_ull = ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_ulonglong
+        dp, vp = ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
+        L.jne_version.restype = c_int
+        L.jne_eigen_count.argtypes = [c_int, c_int]
+        L.jne_open.argtypes = [c_int, c_ull, ctypes.POINTER(vp)]
+        L.jne_close.argtypes = [vp]
+        L.jne_close.restype = None
+        L.jne_last_error.argtypes = [vp]
+        L.jne_last_error.restype = ctypes.c_char_p
+        L.jne_set_chunk.argtypes = [vp, c_int]
+        L.jne_eigs_from_increments.argtypes = [vp, c_int, c_int, c_int, dp, c_int, c_int, dp]
+        L.jne_eigs_seeded.argtypes = [vp, c_int, c_int, c_int, c_u64, c_u32, c_i64, c_int, dp]
+        L.jne_eigs_seeded_device.argtypes = [vp, c_int, c_int, c_int, c_u64, c_u32, c_i64, c_int, vp, vp]
+        L.jne_eigs_seeded_models.argtypes = [vp, ctypes.POINTER(c_int), c_int, c_int, c_int, c_u64, c_u32, c_i64,
+                                             c_int, ctypes.POINTER(dp)]
+        L.jne_export_increments.argtypes = [vp, c_int, c_int, c_u64, c_u32, c_int, dp, ctypes.POINTER(c_u32)]
+        L.jne_profile.argtypes = [vp, c_int]
+        L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Engine:
+    """One C-ABI context on one CUDA device (jne_open / jne_close)."""
+
+    def __init__(self, device: int = 0, mem_budget_bytes: int = 0, chunk: Optional[int] = None):
+        self._L = lib()
+        h = ctypes.c_void_p()
+        rc = self._L.jne_open(device, mem_budget_bytes, ctypes.byref(h))
+        if rc != JNE_OK:
+            raise JneError(rc, f"jne_open(device={device}) failed: no usable CUDA device")
+        self._h = h
+        if chunk is not None:
+            self._check(self._L.jne_set_chunk(self._h, chunk))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.jne_close(self._h)
+            self._h = None
+
+    def __enter__(self) -> "Engine":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int) -> None:
+        if rc != JNE_OK:
+            raise JneError(rc, self._L.jne_last_error(self._h).decode(errors="replace"))
+
+    def set_chunk(self, chunk: int) -> None:
+        self._check(self._L.jne_set_chunk(self._h, chunk))
+
+    def profile(self, enable: bool = True) -> None:
+        """Bracket every kernel launch with CUDA events on its launching stream."""
+        self._check(self._L.jne_profile(self._h, int(enable)))
+
+    def profile_read(self, reset: bool = True) -> Dict[str, Tuple[float, int]]:
+        """{kernel kind: (summed device ms, launches)} since the last reset."""
+        ms = np.zeros(4)
+        n = (ctypes.c_longlong * 4)()
+        self._check(self._L.jne_profile_read(self._h, _dp(ms), n, int(reset)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(KERNEL_KINDS)}
+
+    def eigs_from_increments(self, model: int, dB: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:
+        """dB: (n_runs, steps, dim) -- each run's dim x steps increment matrix, column-major."""
+        dB = np.ascontiguousarray(dB, dtype=np.float64)
+        n, steps, dim = dB.shape
+        out = np.empty((n, eigen_count(model, dim)))
+        self._check(self._L.jne_eigs_from_increments(self._h, int(model), dim, steps, _dp(dB), n, precision, _dp(out)))
+        return out
+
+    def eigs_seeded(self, model: int, dim: int, steps: int, seed_first: int, n_runs: int,
+                    precision: int = PREC_FP64, base_seed: int = DEFAULT_BASE_SEED) -> np.ndarray:
+        out = np.empty((n_runs, eigen_count(model, dim)))
+        self._check(self._L.jne_eigs_seeded(self._h, int(model), dim, steps, base_seed, seed_first, n_runs,
+                                            precision, _dp(out)))
+        return out
+
+    def eigs_seeded_device(self, model: int, dim: int, steps: int, seed_first: int, n_runs: int, out_ptr: int,
+                           precision: int = PREC_FP64, base_seed: int = DEFAULT_BASE_SEED,
+                           stream: Optional[int] = None) -> None:
+        """Results into the device buffer at out_ptr (n_runs x k doubles)."""
+        self._check(self._L.jne_eigs_seeded_device(self._h, int(model), dim, steps, base_seed, seed_first, n_runs,
+                                                   precision, ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
+
+    def eigs_seeded_models(self, models: Sequence[int], dim: int, steps: int, seed_first: int, n_runs: int,
+                           precision: int = PREC_FP64, base_seed: int = DEFAULT_BASE_SEED) -> Dict[int, np.ndarray]:
+        outs = {int(m): np.empty((n_runs, eigen_count(m, dim))) for m in models}
+        arr = (ctypes.c_int * len(models))(*[int(m) for m in models])
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(models))(*[_dp(outs[int(m)]) for m in models])
+        self._check(self._L.jne_eigs_seeded_models(self._h, arr, len(models), dim, steps, base_seed, seed_first,
+                                                   n_runs, precision, ptrs))
+        return outs
+
+    def export_increments(self, dim: int, steps: int, seed_first: int, n_runs: int,
+                          base_seed: int = DEFAULT_BASE_SEED, words: bool = False) -> Tuple[np.ndarray, Optional[np.ndarray]]:
+        dB = np.empty((n_runs, steps, dim))
+        w = np.empty((n_runs, steps, (dim + 3) // 4, 4), dtype=np.uint32) if words else None
+        wp = w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)) if words else None
+        self._check(self._L.jne_export_increments(self._h, dim, steps, base_seed, seed_first, n_runs, _dp(dB), wp))
+        return dB, w

@@ -1,0 +1,367 @@
+// jne_accum_mixed.cu -- mixed-precision fused accumulation: one warp per run,
+// the Gram contraction on the tensor cores (mma.sync m16n8k8, split TF32).
+//
+// Same contract as the plain FP64 kernel (it replaces rng_matrix.rs:57-141,
+// johansen_statistics.rs:102-197 and the two sum_of_outer_products calls of
+// johansen_statistics.rs:32-33) and writes the same FP64 moment record, always
+// the full record, so one pass serves every model.
+//
+// Time is cut into chunks of `chunk` steps (multiple of 32).  Inside a chunk
+// the walk is taken relative to its value Wc at the chunk start (origin
+// shift): b_tau = W_{c0+tau} - Wc, kept in FP32 with a float-float carry.  The
+// warp accumulates, in FP32 on the tensor cores, the 16 x 32 local Gram
+//     sum_tau G_tau [G_tau; z_tau]',   G = [b (d rows); 1; u; u^2; 0...],
+// with u = tau / chunk.  Each operand is split x = hi + lo with hi = x rounded
+// down to TF32 (19 bits) and every product is hi*hi + hi*lo + lo*hi (three
+// MMAs).  At the chunk end the local Gram is mapped to the global FP64 moments
+// (W = Wc + b, y = yc + h u) by the exact shift identities, in FP64.
+//
+// Fragment layout (PTX ISA, mma.m16n8k8 .tf32): lane (g = lane/4, q = lane%4)
+// holds rows g and g+8 of A at k-slots q and q+4, and column g of B at the same
+// k-slots.  The sum over k does not depend on which time step a k-slot carries,
+// so slot k = q (q+4) of MMA s carries tile step 8q + 2s (8q + 2s + 1): every
+// lane owns 8 consecutive steps, which makes the scan along time cheap, and the
+// A fragment registers double as the B fragments of the G x G tiles.
+#include "jne_kernels.h"
+
+namespace {
+
+constexpr int kMixWarps = 4;
+constexpr int kZS = 36;  // z staging row stride (floats): conflict-free float4 reads
+constexpr int kCS = 33;  // chunk-Gram staging row stride (floats)
+
+__device__ __forceinline__ uint32_t tf32_hi(float x) { return __float_as_uint(x) & 0xFFFFE000u; }
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// acc += A B with A, B given as float values: three MMAs on the TF32 split.
+__device__ __forceinline__ void mma_split(float (&c)[4], float a0, float a1, float a2, float a3, float b0,
+                                          float b1) {
+  const uint32_t ah0 = tf32_hi(a0), ah1 = tf32_hi(a1), ah2 = tf32_hi(a2), ah3 = tf32_hi(a3);
+  const uint32_t bh0 = tf32_hi(b0), bh1 = tf32_hi(b1);
+  const uint32_t al0 = __float_as_uint(a0 - __uint_as_float(ah0)), al1 = __float_as_uint(a1 - __uint_as_float(ah1));
+  const uint32_t al2 = __float_as_uint(a2 - __uint_as_float(ah2)), al3 = __float_as_uint(a3 - __uint_as_float(ah3));
+  const uint32_t bl0 = __float_as_uint(b0 - __uint_as_float(bh0)), bl1 = __float_as_uint(b1 - __uint_as_float(bh1));
+  mma_tf32(c, al0, al1, al2, al3, bh0, bh1);
+  mma_tf32(c, ah0, ah1, ah2, ah3, bl0, bl1);
+  mma_tf32(c, ah0, ah1, ah2, ah3, bh0, bh1);
+}
+
+// Two-sum carry update: (hi, lo) += t.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float t) {
+  const float s = __fadd_rn(hi, t);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+// One 32-step tile of one run.  zrow(f) rows of the staging area hold this
+// tile's increments (zero rows for f >= DIM); see the file comment for the
+// lane <-> (row, step) mapping.
+template <int DIM, bool FULL>
+__device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, int tloc, int nvalid,
+                                          float invL, const float (&cA)[4], const float (&cB)[4],
+                                          float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[4][4]) {
+  float zA[8], zB[8];
+  {
+    const float4 p0 = *reinterpret_cast<const float4*>(&zs[g][8 * q]);
+    const float4 p1 = *reinterpret_cast<const float4*>(&zs[g][8 * q + 4]);
+    const float4 r0 = *reinterpret_cast<const float4*>(&zs[g + 8][8 * q]);
+    const float4 r1 = *reinterpret_cast<const float4*>(&zs[g + 8][8 * q + 4]);
+    zA[0] = p0.x; zA[1] = p0.y; zA[2] = p0.z; zA[3] = p0.w; zA[4] = p1.x; zA[5] = p1.y; zA[6] = p1.z; zA[7] = p1.w;
+    zB[0] = r0.x; zB[1] = r0.y; zB[2] = r0.z; zB[3] = r0.w; zB[4] = r1.x; zB[5] = r1.y; zB[6] = r1.z; zB[7] = r1.w;
+  }
+  // lane totals and the exclusive scan over the 4 lanes of the group
+  float tA = ((zA[0] + zA[1]) + (zA[2] + zA[3])) + ((zA[4] + zA[5]) + (zA[6] + zA[7]));
+  float tB = ((zB[0] + zB[1]) + (zB[2] + zB[3])) + ((zB[4] + zB[5]) + (zB[6] + zB[7]));
+  float xA = tA, xB = tB;
+  {
+    float yA = __shfl_up_sync(0xffffffffu, xA, 1, 4), yB = __shfl_up_sync(0xffffffffu, xB, 1, 4);
+    if (q >= 1) { xA += yA; xB += yB; }
+    yA = __shfl_up_sync(0xffffffffu, xA, 2, 4);
+    yB = __shfl_up_sync(0xffffffffu, xB, 2, 4);
+    if (q >= 2) { xA += yA; xB += yB; }
+  }
+  float eA = __shfl_up_sync(0xffffffffu, xA, 1, 4), eB = __shfl_up_sync(0xffffffffu, xB, 1, 4);
+  if (q == 0) { eA = 0.f; eB = 0.f; }
+  const float tileA = __shfl_sync(0xffffffffu, xA, 3, 4), tileB = __shfl_sync(0xffffffffu, xB, 3, 4);
+
+  // G rows rA = g and rB = g + 8 at the lane's 8 steps
+  float GA[8], GB[8];
+  float pA = cloA + eA, pB = cloB + eB;  // tile-local walk (+ carry low word)
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const float bA = chiA + pA, bB = chiB + pB;
+    pA += zA[j];
+    pB += zB[j];
+    const float u = (float)(tloc + j) * invL;
+    if (DIM >= 8) {
+      GA[j] = bA;
+    } else {
+      GA[j] = fmaf(cA[0], bA, fmaf(fmaf(cA[3], u, cA[2]), u, cA[1]));
+    }
+    GB[j] = fmaf(cB[0], bB, fmaf(fmaf(cB[3], u, cB[2]), u, cB[1]));
+    if (!FULL) {
+      if (8 * q + j >= nvalid) { GA[j] = 0.f; GB[j] = 0.f; }
+    }
+  }
+  ff_add(chiA, cloA, tileA);
+  ff_add(chiB, cloB, tileB);
+
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const int j0 = 2 * s, j1 = 2 * s + 1;
+    mma_split(acc[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
+    if (DIM + 3 > 8) mma_split(acc[1], GA[j0], GB[j0], GA[j1], GB[j1], GB[j0], GB[j1]);
+    mma_split(acc[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
+    if (DIM > 8) mma_split(acc[3], GA[j0], GB[j0], GA[j1], GB[j1], zB[j0], zB[j1]);
+  }
+}
+
+template <int N>
+struct cdiv32 {
+  static constexpr int v = (N + 31) / 32;
+};
+
+template <int DIM, bool EXT>
+__global__ void __launch_bounds__(kMixWarps * JNE_WARP) k_accum_mixed(const jne_accum_args a) {
+  constexpr int d = DIM;
+  constexpr int NQ = (d + 3) / 4;
+  constexpr int NMWW = d * (d + 1) / 2, NMW = 3 * d, NNZW = d * d, NNZ = 2 * d;
+  constexpr int EM = cdiv32<NMWW>::v, EW = cdiv32<NMW>::v, EN = cdiv32<NNZW>::v, EZ = cdiv32<NNZ>::v;
+
+  __shared__ __align__(16) float zs_all[kMixWarps][16][kZS];
+  __shared__ float cm_all[kMixWarps][16][kCS];
+  __shared__ double wc_all[kMixWarps][16];
+  __shared__ double tz_all[kMixWarps][16];
+
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  float (*zs)[kZS] = zs_all[wib];
+  float (*cm)[kCS] = cm_all[wib];
+  double* wc = wc_all[wib];
+  double* tz = tz_all[wib];
+  for (int e = lane; e < 16 * kZS; e += 32) (&zs[0][0])[e] = 0.f;
+  if (lane < 16) tz[lane] = 0.0;
+
+  // G-row coefficients: value = c[0]*b + c[1] + c[2]*u + c[3]*u^2
+  float cA[4], cB[4];
+  {
+    const int r[2] = {g, g + 8};
+    for (int h = 0; h < 2; h++) {
+      float* cc = h ? cB : cA;
+      const int rr = r[h];
+      cc[0] = rr < d ? 1.f : 0.f;
+      cc[1] = rr == d ? 1.f : 0.f;
+      cc[2] = rr == d + 1 ? 1.f : 0.f;
+      cc[3] = rr == d + 2 ? 1.f : 0.f;
+    }
+  }
+  // entries of the global record owned by this lane
+  int ewW[EM];
+#pragma unroll
+  for (int m = 0; m < EM; m++) {
+    int e = lane + 32 * m, aa = 0;
+    if (e < NMWW) {
+      while (e >= d - aa) { e -= d - aa; aa++; }
+      ewW[m] = aa | ((aa + e) << 8);
+    } else {
+      ewW[m] = -1;
+    }
+  }
+
+  const int T = a.steps, L = a.chunk;
+  const float invL = 1.0f / (float)L;
+  const double invT = 1.0 / (double)T;
+  const int nwarps = gridDim.x * kMixWarps;
+  __syncwarp();
+
+  for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps) {
+    const uint32_t seed = a.seed_first + (uint32_t)run;
+    double gW[EM], gM[EW], gN[EN], gZ[EZ];
+#pragma unroll
+    for (int m = 0; m < EM; m++) gW[m] = 0.0;
+#pragma unroll
+    for (int m = 0; m < EW; m++) gM[m] = 0.0;
+#pragma unroll
+    for (int m = 0; m < EN; m++) gN[m] = 0.0;
+#pragma unroll
+    for (int m = 0; m < EZ; m++) gZ[m] = 0.0;
+    if (lane < 16) wc[lane] = 0.0;
+    __syncwarp();
+
+    for (int c0 = 0; c0 < T; c0 += L) {
+      const int Lc = min(L, T - c0);
+      float acc[4][4];
+#pragma unroll
+      for (int n = 0; n < 4; n++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) acc[n][r] = 0.f;
+      float chiA = 0.f, cloA = 0.f, chiB = 0.f, cloB = 0.f;
+
+      for (int t0 = c0; t0 < c0 + Lc; t0 += 32) {
+        // producer: lane = tile step, all d increments of column t0 + lane
+        const int i = t0 + lane;
+        const bool valid = i < T;
+        if (EXT) {
+          const double* src = a.ext + ((size_t)run * T + (valid ? i : 0)) * d;
+#pragma unroll
+          for (int f = 0; f < d; f++) zs[f][lane] = valid ? (float)(src[f] * a.ext_inv_scale) : 0.f;
+        } else {
+#pragma unroll
+          for (int j = 0; j < NQ; j++) {
+            float z[4];
+            jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, a.key0, a.key1, z);
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+              if (4 * j + e < d) zs[4 * j + e][lane] = valid ? z[e] : 0.f;
+          }
+        }
+        __syncwarp();
+        const int nvalid = min(32, T - t0);
+        const int tloc = t0 - c0 + 8 * q;
+        if (nvalid == 32)
+          tile_body<DIM, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc);
+        else
+          tile_body<DIM, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc);
+        __syncwarp();
+      }
+
+      // ---- chunk end: stage the local Gram and the chunk totals ----
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        cm[g][8 * n + 2 * q] = acc[n][0];
+        cm[g][8 * n + 2 * q + 1] = acc[n][1];
+        cm[g + 8][8 * n + 2 * q] = acc[n][2];
+        cm[g + 8][8 * n + 2 * q + 1] = acc[n][3];
+      }
+      if (q == 0) {
+        if (g < d) tz[g] = (double)chiA + (double)cloA;
+        if (g + 8 < d) tz[g + 8] = (double)chiB + (double)cloB;
+      }
+      __syncwarp();
+      // ---- FP64 merge: W = Wc + b, y = yc + h u ----
+      const double Lcd = (double)Lc, Ld = (double)L;
+      const double yc = (double)(c0 + 1) * invT, h = Ld * invT;
+      const double P1 = 0.5 * Lcd * (Lcd - 1.0) / Ld;
+      const double P2 = (Lcd - 1.0) * Lcd * (2.0 * Lcd - 1.0) / (6.0 * Ld * Ld);
+      const double e1[3] = {0.0, h, 2.0 * yc * h}, e0[3] = {1.0, yc, yc * yc}, e2[3] = {0.0, 0.0, h * h};
+      const double cWp[3] = {Lcd, Lcd * yc + h * P1, Lcd * yc * yc + 2.0 * yc * h * P1 + h * h * P2};
+#pragma unroll
+      for (int m = 0; m < EM; m++) {
+        if (ewW[m] >= 0) {
+          const int p = ewW[m] & 0xff, r = ewW[m] >> 8;
+          const double wp = wc[p], wr = wc[r];
+          gW[m] += Lcd * wp * wr + wp * (double)cm[d][r] + (double)cm[d][p] * wr + (double)cm[p][r];
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < EW; m++) {
+        const int e = lane + 32 * m;
+        if (e < NMW) {
+          const int p = e / d, r = e - p * d;
+          gM[m] += cWp[p] * wc[r] + e0[p] * (double)cm[d][r] + e1[p] * (double)cm[d + 1][r] +
+                   e2[p] * (double)cm[d + 2][r];
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < EN; m++) {
+        const int e = lane + 32 * m;
+        if (e < NNZW) {
+          const int za = e / d, wb = e - za * d;
+          gN[m] += tz[za] * wc[wb] + (double)cm[wb][16 + za];
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < EZ; m++) {
+        const int e = lane + 32 * m;
+        if (e < NNZ) {
+          const int p = 1 + e / d, za = e - (p - 1) * d;
+          gZ[m] += e0[p] * tz[za] + e1[p] * (double)cm[d + 1][16 + za] + e2[p] * (double)cm[d + 2][16 + za];
+        }
+      }
+      __syncwarp();
+      if (lane < d) wc[lane] += tz[lane];
+      __syncwarp();
+    }
+
+    // ---- write the record ----
+    double* mom = a.mom;
+    const size_t ld = (size_t)a.mom_ld;
+#pragma unroll
+    for (int m = 0; m < EM; m++)
+      if (ewW[m] >= 0) mom[(size_t)jne_slot_MWW(ewW[m] & 0xff, ewW[m] >> 8, d) * ld + run] = gW[m];
+#pragma unroll
+    for (int m = 0; m < EW; m++) {
+      const int e = lane + 32 * m;
+      if (e < NMW) mom[(size_t)(jne_slot_MW1(0, d) + e) * ld + run] = gM[m];  // MW1, MWy, MWyy contiguous
+    }
+#pragma unroll
+    for (int m = 0; m < EN; m++) {
+      const int e = lane + 32 * m;
+      if (e < NNZW) mom[(size_t)(jne_slot_NzW(0, 0, d) + e) * ld + run] = gN[m];
+    }
+#pragma unroll
+    for (int m = 0; m < EZ; m++) {
+      const int e = lane + 32 * m;
+      if (e < NNZ) mom[(size_t)(jne_slot_Nzy(0, d) + e) * ld + run] = gZ[m];  // Nzy, Nzyy contiguous
+    }
+    if (lane < d) mom[(size_t)jne_slot_Nz1(lane, d) * ld + run] = wc[lane];
+    __syncwarp();
+  }
+}
+
+// Persistent grid: exactly the resident blocks (so every warp strides over the
+// same number of runs, +-1), or fewer when the batch is small.
+template <typename K>
+int resident_grid(K kernel, int threads, size_t shm, int sms, int n_runs, int warps_per_block) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, shm) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const int needed = (n_runs + warps_per_block - 1) / warps_per_block;
+  const int full = per_sm * sms;
+  return needed < full ? needed : full;
+}
+
+template <int DIM>
+cudaError_t launch_dim(const jne_accum_args& a, int sms, cudaStream_t st) {
+  const int threads = kMixWarps * JNE_WARP;
+  if (a.ext) {
+    auto k = k_accum_mixed<DIM, true>;
+    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a);
+  } else {
+    auto k = k_accum_mixed<DIM, false>;
+    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, int sms, cudaStream_t st) {
+  if (a.n_runs <= 0) return cudaSuccess;
+  if (a.chunk <= 0 || a.chunk % 32 != 0) return cudaErrorInvalidValue;
+  switch (a.dim) {
+    case 1: return launch_dim<1>(a, sms, st);
+    case 2: return launch_dim<2>(a, sms, st);
+    case 3: return launch_dim<3>(a, sms, st);
+    case 4: return launch_dim<4>(a, sms, st);
+    case 5: return launch_dim<5>(a, sms, st);
+    case 6: return launch_dim<6>(a, sms, st);
+    case 7: return launch_dim<7>(a, sms, st);
+    case 8: return launch_dim<8>(a, sms, st);
+    case 9: return launch_dim<9>(a, sms, st);
+    case 10: return launch_dim<10>(a, sms, st);
+    case 11: return launch_dim<11>(a, sms, st);
+    case 12: return launch_dim<12>(a, sms, st);
+    default: return cudaErrorInvalidValue;
+  }
+}

@@ -1,0 +1,109 @@
+// jne_common.cuh -- shared device definitions: counter-based increments,
+// the per-run moment record, and the argument block of the accumulation kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define JNE_MAX_DIM 12
+#define JNE_MAX_K 13
+#define JNE_WARP 32
+
+// ---------------------------------------------------------------------------
+// Counter-based increments (Philox4x32-10, Salmon et al., SC'11).
+//
+// The standard normal z[f] drawn for step s (1..T) of run `seed` in the
+// (base seed, dim) stream comes from Philox block (s, f/4, seed, 0) under
+// key (lo32(base), hi32(base) ^ (0x4A4E0000 | dim)), word pair (f%4)/2, via
+// Box-Muller.  A run is a pure function of (base seed, dim, seed, s): the model
+// is not part of the key, so -- as in the reference, where
+// calculate_eigenvalues(dim, steps, seed, model) draws the same Brownian matrix
+// for every model (johansen_statistics.rs:59-78) -- all five models see the same
+// path for a given seed.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void jne_philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                  uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// u in (0,1): the top 24 bits of a word plus half an ulp (exact in float).
+__device__ __forceinline__ float jne_u01(uint32_t x) {
+  return __fmaf_rn((float)(x >> 8), 5.9604644775390625e-08f, 2.98023223876953125e-08f);
+}
+
+// Box-Muller pair: r = sqrt(-2 ln u(a)), theta = 2 pi u(b) - pi.  The hardware
+// approximations of log2/sin/cos are used; every rounding step is an explicit
+// _rn intrinsic so no caller can fuse it into a different FMA, which keeps the
+// generated values identical in every kernel that draws them.
+__device__ __forceinline__ void jne_box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
+  const float l2 = __log2f(jne_u01(a));                        // log2(u) < 0
+  const float r = __fsqrt_rn(__fmul_rn(-1.3862943611198906f, l2));  // -2 ln 2 * log2(u)
+  const float th = __fmaf_rn(jne_u01(b), 6.2831853071795865f, -3.1415926535897932f);
+  float s, c;
+  __sincosf(th, &s, &c);
+  z0 = __fmul_rn(r, c);
+  z1 = __fmul_rn(r, s);
+}
+
+// The four normals of quad j (features 4j..4j+3) of step s.
+__device__ __forceinline__ void jne_normal_quad(uint32_t s, uint32_t j, uint32_t seed, uint32_t k0, uint32_t k1,
+                                                float z[4]) {
+  uint32_t w[4];
+  jne_philox4x32_10(s, j, seed, 0u, k0, k1, w);
+  jne_box_muller(w[0], w[1], z[0], z[1]);
+  jne_box_muller(w[2], w[3], z[2], z[3]);
+}
+
+// ---------------------------------------------------------------------------
+// Per-run moment record (FP64), in units of the unscaled walk W_i = sum_{s<=i} z_s
+// (B = zscale * W, dB = zscale * z).  Column i = 0..T-1 pairs W_i (B_{t-1})
+// with the increment z_{i+1} and the time point y_i = (i+1)/T.
+//   [0, d(d+1)/2)        MWW[a][b] = sum W_a W_b        (a <= b, row-major upper)
+//   +d                   MW1[a]    = sum W_a
+//   +d                   MWy[a]    = sum y W_a
+//   +d                   MWyy[a]   = sum y^2 W_a
+//   +d*d                 NzW[a][b] = sum z_a W_b        (a: increment, b: walk)
+//   +d                   Nz1[a]    = sum z_a = W_T
+//   +d                   Nzy[a]    = sum y z_a
+//   +d                   Nzyy[a]   = sum y^2 z_a
+// The record is stored structure-of-arrays: value(slot, run) = mom[slot * ld + run].
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int jne_tri(int a, int b, int d) {  // a <= b
+  return a * d - (a * (a - 1)) / 2 + (b - a);
+}
+__host__ __device__ __forceinline__ int jne_slot_MWW(int a, int b, int d) {
+  return a <= b ? jne_tri(a, b, d) : jne_tri(b, a, d);
+}
+__host__ __device__ __forceinline__ int jne_slot_MW1(int a, int d) { return d * (d + 1) / 2 + a; }
+__host__ __device__ __forceinline__ int jne_slot_MWy(int a, int d) { return d * (d + 1) / 2 + d + a; }
+__host__ __device__ __forceinline__ int jne_slot_MWyy(int a, int d) { return d * (d + 1) / 2 + 2 * d + a; }
+__host__ __device__ __forceinline__ int jne_slot_NzW(int a, int b, int d) { return d * (d + 1) / 2 + 3 * d + a * d + b; }
+__host__ __device__ __forceinline__ int jne_slot_Nz1(int a, int d) { return d * (d + 1) / 2 + 3 * d + d * d + a; }
+__host__ __device__ __forceinline__ int jne_slot_Nzy(int a, int d) { return d * (d + 1) / 2 + 4 * d + d * d + a; }
+__host__ __device__ __forceinline__ int jne_slot_Nzyy(int a, int d) { return d * (d + 1) / 2 + 5 * d + d * d + a; }
+__host__ __device__ __forceinline__ int jne_record_slots(int d) { return d * (d + 1) / 2 + 6 * d + d * d; }
+
+// Argument block of one accumulation launch: runs [0, n_runs) of one
+// (model, dim, steps) request; run r uses seed seed_first + r.
+struct jne_accum_args {
+  int model, dim, steps, n_runs;
+  uint32_t seed_first, key0, key1;
+  int chunk;                 // mixed kernel: steps per FP32 chunk (multiple of 32)
+  const double* ext;         // explicit increments [run][step][dim] (already scaled), or null
+  double ext_inv_scale;      // mixed kernel: z = dB * ext_inv_scale when reading ext
+  double* mom;               // moment records, SoA
+  long long mom_ld;          // leading dimension (>= n_runs)
+  unsigned int* status;      // device status word (bit flags), may be null
+};
+
+// Status bits a kernel may raise (never a trap).
+#define JNE_DEV_BAD_ARGS 0x1u
+#define JNE_DEV_NOT_SPD 0x2u

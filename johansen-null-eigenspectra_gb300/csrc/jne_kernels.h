@@ -1,0 +1,27 @@
+// jne_kernels.h -- host-side launch wrappers of the device kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "jne_common.cuh"
+
+// Deterministic time sums Y[p] = sum_{i=0}^{T-1} ((i+1)/T)^p, p = 0..4.
+struct jne_time_sums {
+  double Y[5];
+};
+
+// Argument block of the finalize kernel.
+struct jne_finalize_args {
+  int model, dim, steps, n_runs;
+  double zscale;            // B = zscale * W, dB = zscale * z
+  jne_time_sums ts;
+  const double* mom;        // moment records (SoA)
+  long long mom_ld;
+  double* out;              // n_runs x k eigenvalues, descending
+  unsigned int* status;
+};
+
+cudaError_t jne_launch_accum_f64(const jne_accum_args& a, const int4* ent, int nent, int sms, cudaStream_t st);
+int jne_build_f64_entries(int model, int d, int4* out, int cap);
+cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, int sms, cudaStream_t st);
+cudaError_t jne_launch_finalize(const jne_finalize_args& f, int sms, cudaStream_t st);
+cudaError_t jne_launch_export(int dim, int steps, int n_runs, uint32_t seed_first, uint32_t key0, uint32_t key1,
+                              double scale, double* out, uint32_t* words, cudaStream_t st);

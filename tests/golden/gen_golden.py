@@ -1,0 +1,50 @@
+"""Generates tests/golden/golden_eigs.npz: per-run eigenvalues of the reference
+algorithm (dense F construction, LAPACK dggev through scipy -- the routine the
+reference binds, johansen_statistics.rs:35-44) on fixed increment matrices.
+
+The reference crate is Rust and cannot be built in this image (no cargo/rustc,
+no system LAPACK), so the fixture is produced by the oracle's numpy/scipy twin
+(oracle/jne_oracle.py), whose sub-steps are pinned by the reference's own
+known-answer tests (reference_known_answers.json).
+
+Run from the repository root:  python tests/golden/gen_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import jne_oracle as o  # noqa: E402
+
+CASES = [(1, 11), (1, 200), (1, 1000), (2, 11), (2, 200), (2, 1000), (3, 11), (3, 200), (3, 1000),
+         (5, 333), (8, 257), (12, 16), (12, 200), (12, 1000)]
+RUNS = 2
+
+
+def load_increments(z: np.ndarray) -> np.ndarray:
+    """(runs, steps, dim) float32 normals -> float64 increments sqrt(1/steps) * z."""
+    return z.astype(np.float64) * np.sqrt(1.0 / z.shape[1])
+
+
+def main() -> None:
+    rng = np.random.default_rng(20240611)
+    out = {}
+    for dim, steps in CASES:
+        # increments dB = sqrt(1/steps) * z with z stored as float32 (see load_increments)
+        z = rng.standard_normal((RUNS, steps, dim)).astype(np.float32)
+        out[f"z_d{dim}_T{steps}"] = z
+        dB = load_increments(z)
+        for model in range(5):
+            if steps <= o.eigen_count(model, dim) + 1:
+                continue  # S11 singular: the reference returns inf/NaN there
+            eig = np.stack([o.eigs_dense(model, dB[r].T) for r in range(RUNS)])
+            out[f"eig_m{model}_d{dim}_T{steps}"] = eig
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_eigs.npz")
+    np.savez_compressed(path, **out)
+    print(path, len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

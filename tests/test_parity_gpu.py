@@ -1,0 +1,157 @@
+"""Parity of the sm_103a kernels with the CPU oracle, through the C ABI.
+
+Tolerances (normwise: max |got - ref| / max |ref| per run):
+  plain FP64 kernel   1e-9
+  mixed kernel        2e-6 per run at the sizes below; at dim 12, T 10^4 the
+                      max-eigenvalue and trace errors against the FP64 kernel on
+                      identical seeds must stay <= 1e-6 (relative).
+"""
+import numpy as np
+import pytest
+
+from conftest import normwise_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-9
+TOL_MIXED = 2e-6
+
+
+def test_philox_words_bit_exact(engine, oracle):
+    for dim in (1, 5, 12):
+        _, words = engine.export_increments(dim, 70, 11, 3, words=True)
+        for r in range(3):
+            ref = oracle.c_philox_words(oracle.DEFAULT_BASE_SEED, dim, 11 + r, 70)
+            assert np.array_equal(words[r], ref), dim
+
+
+def test_normals_match_oracle(engine, oracle):
+    dim, steps = 12, 500
+    dB, _ = engine.export_increments(dim, steps, 100, 4)
+    for r in range(4):
+        z = oracle.c_normals(oracle.DEFAULT_BASE_SEED, dim, 100 + r, steps)
+        assert np.max(np.abs(dB[r] * np.sqrt(steps) - z)) < 1e-4
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL_FP64), (1, TOL_MIXED)], ids=["fp64", "mixed"])
+def test_golden_fixture(engine, golden, precision, tol):
+    cases, eigs = golden
+    for (model, dim, steps), ref in eigs.items():
+        got = engine.eigs_from_increments(model, cases[(dim, steps)], precision=precision)
+        assert normwise_err(got, ref) < tol, (model, dim, steps)
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL_FP64), (1, TOL_MIXED)], ids=["fp64", "mixed"])
+def test_seeded_path_matches_oracle_on_its_increments(engine, oracle, precision, tol):
+    for dim in (1, 2, 5, 9, 12):
+        for steps in (37, 1000):
+            dB, _ = engine.export_increments(dim, steps, 1, 4)
+            for model in range(5):
+                if steps <= oracle.eigen_count(model, dim) + 1:
+                    continue
+                ref = oracle.c_eigs_from_increments(model, dB)
+                got = engine.eigs_seeded(model, dim, steps, 1, 4, precision=precision)
+                assert normwise_err(got, ref) < tol, (model, dim, steps)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_all_models_in_one_pass_equal_single_model_calls(engine, precision):
+    outs = engine.eigs_seeded_models(range(5), 4, 300, 1, 16, precision=precision)
+    for m in range(5):
+        single = engine.eigs_seeded(m, 4, 300, 1, 16, precision=precision)
+        assert np.array_equal(outs[m], single), m
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_run_result_independent_of_batch_and_repeatable(engine, precision):
+    big = engine.eigs_seeded(3, 7, 777, 1, 40, precision=precision)
+    small = engine.eigs_seeded(3, 7, 777, 11, 5, precision=precision)
+    assert np.array_equal(big[10:15], small)
+    assert np.array_equal(big, engine.eigs_seeded(3, 7, 777, 1, 40, precision=precision))
+
+
+@pytest.mark.parametrize("steps", [2, 3, 31, 32, 33, 63, 255, 257, 300])
+def test_ragged_step_counts(engine, oracle, steps):
+    for dim in (1, 2, 12):
+        dB, _ = engine.export_increments(dim, steps, 5, 3)
+        for model in range(5):
+            if steps <= oracle.eigen_count(model, dim) + 1:
+                continue
+            ref = oracle.c_eigs_from_increments(model, dB)
+            for precision, tol in ((0, TOL_FP64), (1, 1e-5)):
+                got = engine.eigs_seeded(model, dim, steps, 5, 3, precision=precision)
+                assert normwise_err(got, ref) < tol, (model, dim, steps, precision)
+
+
+def test_singular_s11_is_reported(engine, jne):
+    # steps = 1: F = B_0 = 0, so S11 = 0 (the reference's dggev returns inf/NaN here)
+    with pytest.raises(jne.JneError) as ei:
+        engine.eigs_seeded(0, 1, 1, 1, 2)
+    assert ei.value.code == jne.JNE_ERR_NUMERIC
+
+
+def test_empty_batch(engine):
+    assert engine.eigs_seeded(0, 3, 100, 1, 0).shape == (0, 3)
+
+
+def test_bad_arguments(engine, jne):
+    for args in ((0, 13, 100), (5, 2, 100), (0, 2, 0), (-1, 2, 100)):
+        with pytest.raises(jne.JneError) as ei:
+            engine.eigs_seeded(args[0], args[1], args[2], 1, 1)
+        assert ei.value.code == jne.JNE_ERR_ARG
+    with pytest.raises(jne.JneError) as ei:
+        engine.eigs_seeded(0, 2, 100, 1, 1, precision=7)
+    assert ei.value.code == jne.JNE_ERR_ARG
+    with pytest.raises(jne.JneError) as ei:  # seed range past u32::MAX
+        engine.eigs_seeded(0, 2, 100, 2**32 - 2, 5)
+    assert ei.value.code == jne.JNE_ERR_ARG
+    with pytest.raises(jne.JneError) as ei:
+        engine.set_chunk(100)
+    assert ei.value.code == jne.JNE_ERR_ARG
+
+
+def test_budget_is_enforced(jne):
+    with jne.Engine(0, mem_budget_bytes=4096) as small:
+        with pytest.raises(jne.JneError) as ei:
+            small.eigs_seeded(0, 12, 100, 1, 10)
+        assert ei.value.code == jne.JNE_ERR_BUDGET
+        with pytest.raises(jne.JneError) as ei:
+            small.eigs_from_increments(0, np.zeros((4, 100, 12)))
+        assert ei.value.code == jne.JNE_ERR_BUDGET
+
+
+def test_chunk_length_changes_only_rounding(jne):
+    with jne.Engine(0, chunk=64) as a, jne.Engine(0, chunk=1024) as b:
+        x = a.eigs_seeded(4, 6, 3000, 1, 8, precision=1)
+        y = b.eigs_seeded(4, 6, 3000, 1, 8, precision=1)
+        assert normwise_err(x, y) < TOL_MIXED
+
+
+def test_full_size_mixed_error_vs_fp64(engine):
+    """dim 12, T 10^4 on identical seeds: mixed max-eig and trace within 1e-6 of FP64."""
+    for model in range(5):
+        f = engine.eigs_seeded(model, 12, 10_000, 1, 256, precision=0)
+        m = engine.eigs_seeded(model, 12, 10_000, 1, 256, precision=1)
+        maxeig = np.max(np.abs(m[:, 0] - f[:, 0]) / f[:, 0])
+        trace = np.max(np.abs(m.sum(1) - f.sum(1)) / f.sum(1))
+        assert maxeig <= 1e-6 and trace <= 1e-6, (model, maxeig, trace)
+
+
+def test_distribution_matches_cpu_oracle(engine, oracle):
+    """Independent samples (different base seeds): two-sample KS and the
+    1/5/10/50/90/95/99% quantiles of trace and max-eig (simulation_analyzers.rs rule)."""
+    from scipy.stats import ks_2samp
+
+    n, dim, steps = 3000, 2, 1000
+    for model in (0, 4):
+        for precision in (0, 1):
+            gpu = engine.eigs_seeded(model, dim, steps, 1, n, precision=precision)
+            cpu = oracle.c_eigs_seeded(model, dim, steps, 1, n, n_threads=8, base_seed=12345)
+            for stat in (lambda e: e.sum(1), lambda e: e.max(1)):
+                a, b = np.sort(stat(gpu)), np.sort(stat(cpu))
+                assert ks_2samp(a, b).pvalue > 1e-3
+                for p in (0.01, 0.05, 0.1, 0.5, 0.9, 0.95, 0.99):
+                    qa, qb = oracle.percentile_value(a, p), oracle.percentile_value(b, p)
+                    # Monte Carlo error of a quantile: ~ sqrt(p(1-p)/n) / density; compare in rank space
+                    rank_b = np.searchsorted(b, qa) / n
+                    assert abs(rank_b - p) < 5 * np.sqrt(p * (1 - p) / n) + 2.0 / n, (model, p, qa, qb)
