@@ -314,7 +314,7 @@ def main() -> None:
     ap.add_argument("--fp64-runs", type=int, default=20_000)
     ap.add_argument("--err-runs", type=int, default=2_000)
     ap.add_argument("--cpu-runs", type=int, default=None, help="CPU sample runs per model (0 = skip)")
-    ap.add_argument("--chunk", type=int, default=256)
+    ap.add_argument("--chunk", type=int, default=0, help="steps per FP32 chunk (0: adaptive, 256 at T=10k)")
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per accumulation launch")
     ap.add_argument("--rng-peak", type=float, default=1.016e12, help="measured Philox+Box-Muller normals/s")
     args = ap.parse_args()

@@ -113,6 +113,54 @@ int jne_profile_read(jne_context* ctx, double* ms, long long* launches, int rese
 int jne_export_increments(jne_context* ctx, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
                           int n_runs, double* dB_out, uint32_t* words_out);
 
+/* ---- EIGENVALS_V6 files (src/data_storage/{writer,reader,uleb128}.rs) ---- */
+typedef struct jne_dat_writer jne_dat_writer;
+
+/* Opens `path` for appending (writer.rs:28-178).  A new file gets the 18-byte
+ * header.  An existing file must carry the same (model, dim, steps), else
+ * JNE_ERR_FORMAT ("Model mismatch: file has model X, expected Y", ...); a file
+ * with a foreign magic header is recreated; a complete file's EOF trailer is
+ * stripped.  *existing (may be null) receives the records already present. */
+int jne_dat_open(const char* path, int model, int dim, uint32_t steps, jne_dat_writer** out, int64_t* existing);
+
+/* Appends n records (seeds[r], eigs[r*k .. r*k+k-1]) (writer.rs:206-259): k <= 255
+ * and the same for every record of the file, else JNE_ERR_FORMAT. */
+int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs, int64_t n, int k);
+
+/* Writes the EOF trailer (count, eigenvalues per record) and closes (writer.rs:262-302). */
+int jne_dat_finish(jne_dat_writer* w);
+
+/* Closes without a trailer, as an interrupted run leaves the file; readers
+ * recover such files by scanning (reader.rs:157-216). */
+void jne_dat_abandon(jne_dat_writer* w);
+
+/* Reads a file (reader.rs:23-216): header fields, record count *n and
+ * eigenvalues per record *k; when seeds and eigs are non-null and cap >= *n,
+ * also the records (eigs is n x k).  Any output pointer may be null. */
+int jne_dat_read(const char* path, int* model, int* dim, uint32_t* steps, int64_t* n, int* k, uint32_t* seeds,
+                 double* eigs, int64_t cap);
+
+/* message of this thread's last failed jne_dat_* / jne_simulation_* / jne_percentiles call */
+const char* jne_dat_last_error(void);
+
+/* ---- EigenvalueSimulation (src/data_storage/simulation.rs, parallel_compute.rs:150-232) ---- */
+
+/* "<data_dir>/eigenvalues_model{m}_dim{d}_steps{T}.dat" (simulation.rs:98-122);
+ * data_dir null or empty means "data". */
+int jne_simulation_filename(const char* data_dir, int model, int dim, int steps, char* buf, size_t cap);
+
+/* Runs or resumes a simulation: the seeds 1..=num_runs missing from the file
+ * are computed on the GPU and appended, then the trailer is written.  A file
+ * with other (model, dim, steps) is removed and recreated
+ * (parallel_compute.rs:155-180).  The directory is created on demand. */
+int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int dim, int steps, int64_t num_runs,
+                       int precision, uint64_t base_seed, int quiet);
+
+/* Percentiles (simulation_analyzers.rs:4-81) of the trace (stat 0) or the
+ * largest eigenvalue (stat 1) of n records of k eigenvalues: linear
+ * interpolation at rank p * (n - 1) of the sorted statistic; NaN when n == 0. */
+int jne_percentiles(const double* eigs, int64_t n, int k, int stat, const double* ps, int np, double* out);
+
 #ifdef __cplusplus
 }
 #endif

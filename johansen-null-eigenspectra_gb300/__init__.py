@@ -31,6 +31,8 @@ EXPORTS = (
     "jne_version", "jne_eigen_count", "jne_open", "jne_close", "jne_last_error", "jne_set_chunk",
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
     "jne_export_increments", "jne_profile", "jne_profile_read",
+    "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
+    "jne_simulation_filename", "jne_simulation_run", "jne_percentiles",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
 
@@ -132,6 +134,17 @@ def lib() -> ctypes.CDLL:
         L.jne_export_increments.argtypes = [vp, c_int, c_int, c_u64, c_u32, c_int, dp, ctypes.POINTER(c_u32)]
         L.jne_profile.argtypes = [vp, c_int]
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
+        u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
+        L.jne_dat_open.argtypes = [ctypes.c_char_p, c_int, c_int, c_u32, ctypes.POINTER(vp), i64p]
+        L.jne_dat_append.argtypes = [vp, u32p, dp, c_i64, c_int]
+        L.jne_dat_finish.argtypes = [vp]
+        L.jne_dat_abandon.argtypes = [vp]
+        L.jne_dat_abandon.restype = None
+        L.jne_dat_read.argtypes = [ctypes.c_char_p, ip, ip, u32p, i64p, ip, u32p, dp, c_i64]
+        L.jne_dat_last_error.restype = ctypes.c_char_p
+        L.jne_simulation_filename.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, ctypes.c_char_p, ctypes.c_size_t]
+        L.jne_simulation_run.argtypes = [vp, ctypes.c_char_p, c_int, c_int, c_int, c_i64, c_int, c_u64, c_int]
+        L.jne_percentiles.argtypes = [dp, c_i64, c_int, c_int, dp, c_int, dp]
         _lib = L
     return _lib
 
@@ -226,3 +239,167 @@ class Engine:
         wp = w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)) if words else None
         self._check(self._L.jne_export_increments(self._h, dim, steps, base_seed, seed_first, n_runs, _dp(dB), wp))
         return dB, w
+
+
+# --------------------------------------------------------------------------
+# EIGENVALS_V6 files, percentiles and the EigenvalueSimulation mirror
+# --------------------------------------------------------------------------
+class DatError(JneError):
+    """A failed jne_dat_* / jne_simulation_* / jne_percentiles call (std::io::Error in the reference)."""
+
+
+def _dat_check(rc: int) -> None:
+    if rc != JNE_OK:
+        raise DatError(rc, lib().jne_dat_last_error().decode(errors="replace"))
+
+
+class Records:
+    """(seed, eigenvalues) records backed by two arrays: a sequence of tuples like
+    the reference's Vec<(u32, Vec<f64>)>, with .seeds (uint32) and .eigs (n x k)."""
+
+    def __init__(self, seeds: np.ndarray, eigs: np.ndarray):
+        self.seeds, self.eigs = seeds, eigs
+
+    def __len__(self) -> int:
+        return len(self.seeds)
+
+    def __getitem__(self, i):
+        return int(self.seeds[i]), self.eigs[i]
+
+    def __iter__(self):
+        return ((int(s), e) for s, e in zip(self.seeds, self.eigs))
+
+    def sorted_by_seed(self) -> "Records":
+        o = np.argsort(self.seeds, kind="stable")
+        return Records(self.seeds[o], self.eigs[o])
+
+
+class DatWriter:
+    """Append-only writer (writer.rs:16-303)."""
+
+    def __init__(self, path: str, model: int, dim: int, steps: int):
+        L = lib()
+        h, existing = ctypes.c_void_p(), ctypes.c_int64()
+        _dat_check(L.jne_dat_open(os.fsencode(path), int(model), dim, steps, ctypes.byref(h), ctypes.byref(existing)))
+        self._h, self.existing = h, existing.value
+
+    def append(self, seeds: Sequence[int], eigs: np.ndarray) -> None:
+        s = np.ascontiguousarray(seeds, dtype=np.uint32)
+        e = np.ascontiguousarray(eigs, dtype=np.float64).reshape(len(s), -1)
+        _dat_check(lib().jne_dat_append(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _dp(e),
+                                        len(s), e.shape[1]))
+
+    def append_eigenvalues(self, seed: int, eigenvalues: Sequence[float]) -> None:
+        self.append([seed], np.asarray(eigenvalues, dtype=np.float64).reshape(1, -1))
+
+    def finish(self) -> None:
+        h, self._h = self._h, None
+        _dat_check(lib().jne_dat_finish(h))
+
+    def abandon(self) -> None:
+        """Close without the EOF trailer (as an interrupted run leaves the file)."""
+        h, self._h = self._h, None
+        lib().jne_dat_abandon(h)
+
+
+def read_dat(path: str) -> Tuple[Records, int, int, int]:
+    """read_append_file (reader.rs:23-73): (records, model, dim, steps)."""
+    L = lib()
+    model, dim, k = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    steps, n = ctypes.c_uint32(), ctypes.c_int64()
+    p = os.fsencode(path)
+    _dat_check(L.jne_dat_read(p, ctypes.byref(model), ctypes.byref(dim), ctypes.byref(steps), ctypes.byref(n),
+                              ctypes.byref(k), None, None, 0))
+    seeds = np.empty(n.value, dtype=np.uint32)
+    eigs = np.empty((n.value, k.value))
+    if n.value:
+        _dat_check(L.jne_dat_read(p, None, None, None, ctypes.byref(n), ctypes.byref(k),
+                                  seeds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _dp(eigs), n.value))
+    return Records(seeds, eigs), model.value, dim.value, steps.value
+
+
+def percentiles(eigs: np.ndarray, stat: str, ps: Sequence[float]) -> List[float]:
+    """simulation_analyzers.rs:4-81 for stat 'trace' (Sum) or 'maxeig' (Max)."""
+    e = np.ascontiguousarray(eigs, dtype=np.float64)
+    e = e.reshape(len(e), -1) if e.size else np.zeros((0, 1))
+    p = np.ascontiguousarray(ps, dtype=np.float64)
+    out = np.empty(len(p))
+    _dat_check(lib().jne_percentiles(_dp(e), len(e), e.shape[1], 0 if stat == "trace" else 1, _dp(p), len(p),
+                                     _dp(out)))
+    return out.tolist()
+
+
+_engine: Optional[Engine] = None
+
+
+def default_engine() -> Engine:
+    global _engine
+    if _engine is None:
+        _engine = Engine(0)
+    return _engine
+
+
+class EigenvalueSimulation:
+    """Mirror of the reference's EigenvalueSimulation (src/data_storage/simulation.rs:11-122).
+
+    Runs go to the GPU (precision JNE_PREC_MIXED by default, JNE_PREC_FP64 on
+    request); records are written to data_dir/eigenvalues_model{m}_dim{d}_steps{T}.dat
+    in the reference's EIGENVALS_V6 format, with the same resume semantics."""
+
+    def __init__(self, model, dim: int, steps: int, num_runs: int, data_dir: str = "data",
+                 precision: int = PREC_MIXED, base_seed: int = DEFAULT_BASE_SEED, engine: Optional[Engine] = None):
+        self.model = JohansenModel(int(model))
+        self.dim, self.steps, self.num_runs = dim, steps, num_runs
+        self.data_dir, self.precision, self.base_seed = data_dir, precision, base_seed
+        self._engine = engine
+
+    @classmethod
+    def new(cls, model, dim: int, steps: int, num_runs: int, **kw) -> "EigenvalueSimulation":
+        return cls(model, dim, steps, num_runs, **kw)
+
+    def _run(self, quiet: bool) -> None:
+        eng = self._engine or default_engine()
+        rc = lib().jne_simulation_run(eng._h, os.fsencode(self.data_dir), int(self.model), self.dim, self.steps,
+                                      self.num_runs, self.precision, self.base_seed, int(quiet))
+        if rc != JNE_OK:
+            # reference: run_model_simulation panics on writer or compute errors
+            raise DatError(rc, lib().jne_dat_last_error().decode(errors="replace"))
+
+    def run_simulation(self) -> None:
+        self._run(False)
+
+    def run_simulation_quiet(self) -> None:
+        self._run(True)
+
+    def get_filename(self, model=None) -> str:
+        m = self.model if model is None else JohansenModel(int(model))
+        os.makedirs(self.data_dir, exist_ok=True)
+        buf = ctypes.create_string_buffer(4096)
+        _dat_check(lib().jne_simulation_filename(os.fsencode(self.data_dir), int(m), self.dim, self.steps, buf, 4096))
+        return buf.value.decode()
+
+    def read_all_data(self) -> Records:
+        return read_dat(self.get_filename(self.model))[0]
+
+    def read_data(self) -> Records:
+        """Records with seed <= num_runs; an error when their count is not num_runs (simulation.rs:61-87)."""
+        allr = self.read_all_data()
+        keep = allr.seeds <= np.uint32(min(self.num_runs, 0xFFFFFFFF))
+        got = Records(allr.seeds[keep], allr.eigs[keep])
+        if len(got) != self.num_runs:
+            m = len(got)
+            raise DatError(JNE_ERR_FORMAT,
+                           f"Data count mismatch: expected {self.num_runs} records, found {m} records. "
+                           "This indicates incomplete simulation data.\nSolutions:\n"
+                           f"1. Use `read_all_data()` to read available data ({m} records)\n"
+                           "2. Run `run_simulation()` to complete the simulation\n"
+                           f"3. Create a new EigenvalueSimulation with num_runs={m} to match existing data")
+        return got
+
+    def calculate_trace_percentiles(self, ps: Sequence[float]) -> List[float]:
+        data = self.read_data()
+        return [] if len(data) == 0 else percentiles(data.eigs, "trace", ps)
+
+    def calculate_maxeig_percentiles(self, ps: Sequence[float]) -> List[float]:
+        data = self.read_data()
+        return [] if len(data) == 0 else percentiles(data.eigs, "maxeig", ps)

@@ -44,7 +44,7 @@ def _stale(srcs) -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     if not force and not _stale(srcs):
         return LIB
     os.makedirs(OBJ, exist_ok=True)

@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(kF64Warps * JNE_WARP)
   }
   const double invT = 1.0 / (double)T;
   const int nq = (d + 3) >> 2;
+  const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
   const int nwarps = gridDim.x * kF64Warps;
   __syncwarp();
 
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(kF64Warps * JNE_WARP)
       } else {
         for (int j = 0; j < nq; j++) {
           float z[4];
-          jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, a.key0, a.key1, z);
+          jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, rk, z);
 #pragma unroll
           for (int e = 0; e < 4; e++) {
             const int f = 4 * j + e;

@@ -41,17 +41,22 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// acc += A B with A, B given as float values: three MMAs on the TF32 split.
-__device__ __forceinline__ void mma_split(float (&c)[4], float a0, float a1, float a2, float a3, float b0,
-                                          float b1) {
+// A B with A, B given as float values, on the TF32 split: the hi*hi product
+// goes to `hh`, the two cross products to `x`.  The tensor core's FP32
+// accumulation truncates, so its error is biased and grows with the number of
+// additions into one accumulator: keeping the (2^11 times smaller) cross terms
+// apart and emptying `hh` after every tile keeps that bias ~10x below a single
+// accumulator per chunk.
+__device__ __forceinline__ void mma_split(float (&hh)[4], float (&x)[4], float a0, float a1, float a2, float a3,
+                                          float b0, float b1) {
   const uint32_t ah0 = tf32_hi(a0), ah1 = tf32_hi(a1), ah2 = tf32_hi(a2), ah3 = tf32_hi(a3);
   const uint32_t bh0 = tf32_hi(b0), bh1 = tf32_hi(b1);
   const uint32_t al0 = __float_as_uint(a0 - __uint_as_float(ah0)), al1 = __float_as_uint(a1 - __uint_as_float(ah1));
   const uint32_t al2 = __float_as_uint(a2 - __uint_as_float(ah2)), al3 = __float_as_uint(a3 - __uint_as_float(ah3));
   const uint32_t bl0 = __float_as_uint(b0 - __uint_as_float(bh0)), bl1 = __float_as_uint(b1 - __uint_as_float(bh1));
-  mma_tf32(c, al0, al1, al2, al3, bh0, bh1);
-  mma_tf32(c, ah0, ah1, ah2, ah3, bl0, bl1);
-  mma_tf32(c, ah0, ah1, ah2, ah3, bh0, bh1);
+  mma_tf32(x, al0, al1, al2, al3, bh0, bh1);
+  mma_tf32(x, ah0, ah1, ah2, ah3, bl0, bl1);
+  mma_tf32(hh, ah0, ah1, ah2, ah3, bh0, bh1);
 }
 
 // Two-sum carry update: (hi, lo) += t.
@@ -69,7 +74,8 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float t) {
 template <int DIM, bool FULL>
 __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, int tloc, int nvalid,
                                           float invL, const float (&cA)[4], const float (&cB)[4],
-                                          float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[4][4]) {
+                                          float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[4][4],
+                                          float (&accx)[4][4]) {
   float zA[8], zB[8];
   {
     const float4 p0 = *reinterpret_cast<const float4*>(&zs[g][8 * q]);
@@ -116,32 +122,43 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   ff_add(chiA, cloA, tileA);
   ff_add(chiB, cloB, tileB);
 
+  float hh[4][4];
+#pragma unroll
+  for (int n = 0; n < 4; n++)
+#pragma unroll
+    for (int r = 0; r < 4; r++) hh[n][r] = 0.f;
 #pragma unroll
   for (int s = 0; s < 4; s++) {
     const int j0 = 2 * s, j1 = 2 * s + 1;
-    mma_split(acc[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
-    if (DIM + 3 > 8) mma_split(acc[1], GA[j0], GB[j0], GA[j1], GB[j1], GB[j0], GB[j1]);
-    mma_split(acc[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
-    if (DIM > 8) mma_split(acc[3], GA[j0], GB[j0], GA[j1], GB[j1], zB[j0], zB[j1]);
+    mma_split(hh[0], accx[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
+    if (DIM + 3 > 8) mma_split(hh[1], accx[1], GA[j0], GB[j0], GA[j1], GB[j1], GB[j0], GB[j1]);
+    mma_split(hh[2], accx[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
+    if (DIM > 8) mma_split(hh[3], accx[3], GA[j0], GB[j0], GA[j1], GB[j1], zB[j0], zB[j1]);
   }
+  // empty the tile's hi*hi accumulator into the chunk sum (round to nearest)
+#pragma unroll
+  for (int n = 0; n < 4; n++)
+#pragma unroll
+    for (int r = 0; r < 4; r++) acc[n][r] = __fadd_rn(acc[n][r], hh[n][r]);
 }
 
-template <int N>
-struct cdiv32 {
-  static constexpr int v = (N + 31) / 32;
-};
-
 template <int DIM, bool EXT>
-__global__ void __launch_bounds__(kMixWarps * JNE_WARP) k_accum_mixed(const jne_accum_args a) {
+__global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4) k_accum_mixed(const jne_accum_args a) {
   constexpr int d = DIM;
   constexpr int NQ = (d + 3) / 4;
-  constexpr int NMWW = d * (d + 1) / 2, NMW = 3 * d, NNZW = d * d, NNZ = 2 * d;
-  constexpr int EM = cdiv32<NMWW>::v, EW = cdiv32<NMW>::v, EN = cdiv32<NNZW>::v, EZ = cdiv32<NNZ>::v;
+  constexpr int NMWW = d * (d + 1) / 2, NMW = 3 * d, NNZW = d * d;
+  constexpr int NREC = NMWW + NMW + NNZW + 3 * d;  // == jne_record_slots(d)
 
   __shared__ __align__(16) float zs_all[kMixWarps][16][kZS];
   __shared__ float cm_all[kMixWarps][16][kCS];
   __shared__ double wc_all[kMixWarps][16];
   __shared__ double tz_all[kMixWarps][16];
+  __shared__ double rec_all[kMixWarps][NREC];   // the run's record: FP64 part
+  __shared__ float rech_all[kMixWarps][NREC];   // ... and float-float centred part
+  __shared__ float recl_all[kMixWarps][NREC];
+  __shared__ double fd_all[kMixWarps][2][16];   // per feature: chunk mean m, Lc * m
+  __shared__ float ff_all[kMixWarps][6][16];    // per feature: centred FP32 chunk moments
+  __shared__ unsigned short mww_pr[NMWW];
 
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int g = lane >> 2, q = lane & 3;
@@ -149,6 +166,17 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP) k_accum_mixed(const jne_
   float (*cm)[kCS] = cm_all[wib];
   double* wc = wc_all[wib];
   double* tz = tz_all[wib];
+  double* rec = rec_all[wib];
+  float* rech = rech_all[wib];
+  float* recl = recl_all[wib];
+  double* mm = fd_all[wib][0];
+  double* lm = fd_all[wib][1];
+  float* sbf = ff_all[wib][0];
+  float* tzfs = ff_all[wib][1];
+  float* cub = ff_all[wib][2];
+  float* cuub = ff_all[wib][3];
+  float* cuz = ff_all[wib][4];
+  float* cuuz = ff_all[wib][5];
   for (int e = lane; e < 16 * kZS; e += 32) (&zs[0][0])[e] = 0.f;
   if (lane < 16) tz[lane] = 0.0;
 
@@ -165,46 +193,40 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP) k_accum_mixed(const jne_
       cc[3] = rr == d + 2 ? 1.f : 0.f;
     }
   }
-  // entries of the global record owned by this lane
-  int ewW[EM];
-#pragma unroll
-  for (int m = 0; m < EM; m++) {
-    int e = lane + 32 * m, aa = 0;
-    if (e < NMWW) {
-      while (e >= d - aa) { e -= d - aa; aa++; }
-      ewW[m] = aa | ((aa + e) << 8);
-    } else {
-      ewW[m] = -1;
-    }
+  // (p, r) of the upper-triangular walk moments, shared by the block
+  for (int e = threadIdx.x; e < NMWW; e += blockDim.x) {
+    int t = e, aa = 0;
+    while (t >= d - aa) { t -= d - aa; aa++; }
+    mww_pr[e] = (unsigned short)(aa | ((aa + t) << 8));
   }
+  __syncthreads();
 
   const int T = a.steps, L = a.chunk;
   const float invL = 1.0f / (float)L;
-  const double invT = 1.0 / (double)T;
+  const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
+  const float invTf = 1.0f / (float)T;
   const int nwarps = gridDim.x * kMixWarps;
-  __syncwarp();
 
   for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps) {
     const uint32_t seed = a.seed_first + (uint32_t)run;
-    double gW[EM], gM[EW], gN[EN], gZ[EZ];
-#pragma unroll
-    for (int m = 0; m < EM; m++) gW[m] = 0.0;
-#pragma unroll
-    for (int m = 0; m < EW; m++) gM[m] = 0.0;
-#pragma unroll
-    for (int m = 0; m < EN; m++) gN[m] = 0.0;
-#pragma unroll
-    for (int m = 0; m < EZ; m++) gZ[m] = 0.0;
+    for (int e = lane; e < NREC; e += 32) {
+      rec[e] = 0.0;
+      rech[e] = 0.f;
+      recl[e] = 0.f;
+    }
     if (lane < 16) wc[lane] = 0.0;
     __syncwarp();
 
     for (int c0 = 0; c0 < T; c0 += L) {
       const int Lc = min(L, T - c0);
-      float acc[4][4];
+      float acc[4][4], accx[4][4];  // chunk sums: hi*hi (emptied per tile) and cross terms
 #pragma unroll
       for (int n = 0; n < 4; n++)
 #pragma unroll
-        for (int r = 0; r < 4; r++) acc[n][r] = 0.f;
+        for (int r = 0; r < 4; r++) {
+          acc[n][r] = 0.f;
+          accx[n][r] = 0.f;
+        }
       float chiA = 0.f, cloA = 0.f, chiB = 0.f, cloB = 0.f;
 
       for (int t0 = c0; t0 < c0 + Lc; t0 += 32) {
@@ -219,7 +241,7 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP) k_accum_mixed(const jne_
 #pragma unroll
           for (int j = 0; j < NQ; j++) {
             float z[4];
-            jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, a.key0, a.key1, z);
+            jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, rk, z);
 #pragma unroll
             for (int e = 0; e < 4; e++)
               if (4 * j + e < d) zs[4 * j + e][lane] = valid ? z[e] : 0.f;
@@ -229,92 +251,103 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP) k_accum_mixed(const jne_
         const int nvalid = min(32, T - t0);
         const int tloc = t0 - c0 + 8 * q;
         if (nvalid == 32)
-          tile_body<DIM, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc);
+          tile_body<DIM, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
         else
-          tile_body<DIM, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc);
+          tile_body<DIM, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
         __syncwarp();
       }
 
       // ---- chunk end: stage the local Gram and the chunk totals ----
 #pragma unroll
       for (int n = 0; n < 4; n++) {
-        cm[g][8 * n + 2 * q] = acc[n][0];
-        cm[g][8 * n + 2 * q + 1] = acc[n][1];
-        cm[g + 8][8 * n + 2 * q] = acc[n][2];
-        cm[g + 8][8 * n + 2 * q + 1] = acc[n][3];
+        cm[g][8 * n + 2 * q] = acc[n][0] + accx[n][0];
+        cm[g][8 * n + 2 * q + 1] = acc[n][1] + accx[n][1];
+        cm[g + 8][8 * n + 2 * q] = acc[n][2] + accx[n][2];
+        cm[g + 8][8 * n + 2 * q + 1] = acc[n][3] + accx[n][3];
       }
       if (q == 0) {
         if (g < d) tz[g] = (double)chiA + (double)cloA;
         if (g + 8 < d) tz[g + 8] = (double)chiB + (double)cloB;
       }
       __syncwarp();
-      // ---- FP64 merge: W = Wc + b, y = yc + h u ----
-      const double Lcd = (double)Lc, Ld = (double)L;
-      const double yc = (double)(c0 + 1) * invT, h = Ld * invT;
-      const double P1 = 0.5 * Lcd * (Lcd - 1.0) / Ld;
-      const double P2 = (Lcd - 1.0) * Lcd * (2.0 * Lcd - 1.0) / (6.0 * Ld * Ld);
-      const double e1[3] = {0.0, h, 2.0 * yc * h}, e0[3] = {1.0, yc, yc * yc}, e2[3] = {0.0, 0.0, h * h};
-      const double cWp[3] = {Lcd, Lcd * yc + h * P1, Lcd * yc * yc + 2.0 * yc * h * P1 + h * h * P2};
-#pragma unroll
-      for (int m = 0; m < EM; m++) {
-        if (ewW[m] >= 0) {
-          const int p = ewW[m] & 0xff, r = ewW[m] >> 8;
-          const double wp = wc[p], wr = wc[r];
-          gW[m] += Lcd * wp * wr + wp * (double)cm[d][r] + (double)cm[d][p] * wr + (double)cm[p][r];
-        }
+      // ---- merge into the run's record: W = m + beta (m = chunk mean of W, sum beta = 0),
+      //      y = ybar + h (u - ubar).  Every moment splits into a "mean" part, a product of
+      //      chunk means (FP64, one FMA per slot), and a centred local part (FP32, small,
+      //      summed across chunks in float-float). ----
+      const jne_chunk_time ct = a.chunk_tab[c0 / L];
+      const float Lcf = (float)Lc, invLcf = 1.0f / Lcf;
+      const float P1f = 0.5f * Lcf * (Lcf - 1.0f) * invL;
+      const float P2f = (Lcf - 1.0f) * Lcf * (2.0f * Lcf - 1.0f) * invL * invL * (1.0f / 6.0f);
+      const float ub = P1f * invLcf;                 // mean of u over the chunk
+      const float sig2 = P2f - P1f * ub;             // sum of (u - ubar)^2
+      const float qbar = sig2 * invLcf;              // mean of (u - ubar)^2
+      const float hf = (float)L * invTf, ybf = (float)ct.ybar;
+      if (lane < d) {
+        const int f = lane;
+        const float Sb = cm[d][f], Sub = cm[d + 1][f], Suub = cm[d + 2][f];
+        const float Suz = cm[d + 1][16 + f], Suuz = cm[d + 2][16 + f];
+        const double m = wc[f] + (double)Sb * ct.inv_lc;
+        mm[f] = m;
+        lm[f] = ct.lc * m;
+        const float tzf = (float)tz[f];
+        sbf[f] = Sb;
+        tzfs[f] = tzf;
+        cub[f] = Sub - ub * Sb;                                              // sum (u-ubar) beta
+        cuub[f] = Suub - 2.0f * ub * Sub + ub * ub * Sb - Sb * invLcf * sig2;  // sum (u-ubar)^2 beta
+        cuz[f] = Suz - ub * tzf;                                             // sum (u-ubar) z
+        cuuz[f] = Suuz - 2.0f * ub * Suz + ub * ub * tzf - qbar * tzf;       // sum ((u-ubar)^2 - qbar) z
       }
-#pragma unroll
-      for (int m = 0; m < EW; m++) {
-        const int e = lane + 32 * m;
-        if (e < NMW) {
-          const int p = e / d, r = e - p * d;
-          gM[m] += cWp[p] * wc[r] + e0[p] * (double)cm[d][r] + e1[p] * (double)cm[d + 1][r] +
-                   e2[p] * (double)cm[d + 2][r];
+      __syncwarp();
+      // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy
+      for (int e = lane; e < NREC; e += 32) {
+        double v64;
+        float v32;
+        if (e < NMWW) {
+          const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
+          v64 = lm[p] * mm[r];
+          v32 = cm[p][r] - sbf[p] * sbf[r] * invLcf;
+        } else if (e < NMWW + NMW) {
+          const int t = e - NMWW, pp = t / d, r = t - pp * d;
+          if (pp == 0) {
+            v64 = lm[r];
+            v32 = 0.f;
+          } else if (pp == 1) {
+            v64 = ct.ybar * lm[r];
+            v32 = hf * cub[r];
+          } else {
+            v64 = ct.y2bar * lm[r];
+            v32 = 2.0f * ybf * hf * cub[r] + hf * hf * cuub[r];
+          }
+        } else if (e < NMWW + NMW + NNZW) {
+          const int t = e - NMWW - NMW, za = t / d, wb = t - za * d;
+          v64 = tz[za] * mm[wb];
+          v32 = cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf;
+        } else if (e < NMWW + NMW + NNZW + d) {
+          v64 = 0.0;  // Nz1: the walk's end point, written from wc
+          v32 = 0.f;
+        } else {
+          const int t = e - NMWW - NMW - NNZW - d, pp = 1 + t / d, za = t - (pp - 1) * d;
+          if (pp == 1) {
+            v64 = ct.ybar * tz[za];
+            v32 = hf * cuz[za];
+          } else {
+            v64 = ct.y2bar * tz[za];
+            v32 = 2.0f * ybf * hf * cuz[za] + hf * hf * cuuz[za];
+          }
         }
-      }
-#pragma unroll
-      for (int m = 0; m < EN; m++) {
-        const int e = lane + 32 * m;
-        if (e < NNZW) {
-          const int za = e / d, wb = e - za * d;
-          gN[m] += tz[za] * wc[wb] + (double)cm[wb][16 + za];
-        }
-      }
-#pragma unroll
-      for (int m = 0; m < EZ; m++) {
-        const int e = lane + 32 * m;
-        if (e < NNZ) {
-          const int p = 1 + e / d, za = e - (p - 1) * d;
-          gZ[m] += e0[p] * tz[za] + e1[p] * (double)cm[d + 1][16 + za] + e2[p] * (double)cm[d + 2][16 + za];
-        }
+        rec[e] += v64;
+        ff_add(rech[e], recl[e], v32);
       }
       __syncwarp();
       if (lane < d) wc[lane] += tz[lane];
       __syncwarp();
     }
 
-    // ---- write the record ----
-    double* mom = a.mom;
+    // ---- write the record (slot order of jne_common.cuh) ----
+    if (lane < d) rec[jne_slot_Nz1(lane, d)] = wc[lane];
+    __syncwarp();
     const size_t ld = (size_t)a.mom_ld;
-#pragma unroll
-    for (int m = 0; m < EM; m++)
-      if (ewW[m] >= 0) mom[(size_t)jne_slot_MWW(ewW[m] & 0xff, ewW[m] >> 8, d) * ld + run] = gW[m];
-#pragma unroll
-    for (int m = 0; m < EW; m++) {
-      const int e = lane + 32 * m;
-      if (e < NMW) mom[(size_t)(jne_slot_MW1(0, d) + e) * ld + run] = gM[m];  // MW1, MWy, MWyy contiguous
-    }
-#pragma unroll
-    for (int m = 0; m < EN; m++) {
-      const int e = lane + 32 * m;
-      if (e < NNZW) mom[(size_t)(jne_slot_NzW(0, 0, d) + e) * ld + run] = gN[m];
-    }
-#pragma unroll
-    for (int m = 0; m < EZ; m++) {
-      const int e = lane + 32 * m;
-      if (e < NNZ) mom[(size_t)(jne_slot_Nzy(0, d) + e) * ld + run] = gZ[m];  // Nzy, Nzyy contiguous
-    }
-    if (lane < d) mom[(size_t)jne_slot_Nz1(lane, d) * ld + run] = wc[lane];
+    for (int e = lane; e < NREC; e += 32) a.mom[(size_t)e * ld + run] = rec[e] + ((double)rech[e] + (double)recl[e]);
     __syncwarp();
   }
 }

@@ -15,7 +15,12 @@ struct jne_context {
   int sms = 0;
   unsigned long long budget = 0;
   unsigned long long in_use = 0;
-  int chunk = 256;
+  int chunk = 0;  // 0: chunk length chosen from the step count
+  jne_chunk_time* d_ctab = nullptr;
+  size_t ctab_cap = 0;
+  std::vector<jne_chunk_time> h_ctab;
+  int ctab_steps = -1, ctab_chunk = -1;  // table currently on the device
+  int ent_model = -2, ent_dim = -1, ent_n = 0;
   cudaStream_t stream = nullptr;
   double* d_mom = nullptr;
   size_t mom_cap = 0;  // doubles
@@ -121,6 +126,15 @@ struct ProfScope {
   }
 };
 
+// Steps per FP32 chunk of the mixed kernel: about T/32, a power of two in
+// [32, 256].  Short paths get short chunks, so that the FP64 chunk means carry
+// most of every moment and the FP32 centred parts stay a small share.
+int adaptive_chunk(int steps) {
+  int L = 32;
+  while (L < 256 && 2 * L * 32 <= steps) L *= 2;
+  return L;
+}
+
 bool valid_model_dim(int model, int dim) { return model >= 0 && model <= 4 && dim >= 1 && dim <= JNE_MAX_DIM; }
 
 jne_time_sums time_sums(int steps) {
@@ -170,7 +184,7 @@ int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uin
   a.seed_first = seed_first;
   a.key0 = key0;
   a.key1 = key1;
-  a.chunk = c->chunk;
+  a.chunk = c->chunk ? c->chunk : adaptive_chunk(steps);
   a.ext = d_ext;
   a.ext_inv_scale = std::sqrt((double)steps);
   a.mom = c->d_mom;
@@ -178,15 +192,41 @@ int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uin
   a.status = c->d_status;
   cudaError_t e;
   if (precision == JNE_PREC_FP64) {
-    int4 host_ent[512];
-    const int nent = jne_build_f64_entries(model, dim, host_ent, 512);
-    int rc = ensure(c, &c->d_ent, &c->ent_cap, 512, "entry table");
-    if (rc) return rc;
-    e = cudaMemcpyAsync(c->d_ent, host_ent, sizeof(int4) * nent, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(c, e, "entry table upload");
+    if (c->ent_model != model || c->ent_dim != dim) {
+      int4 host_ent[512];
+      c->ent_n = jne_build_f64_entries(model, dim, host_ent, 512);
+      int rc = ensure(c, &c->d_ent, &c->ent_cap, 512, "entry table");
+      if (rc) return rc;
+      e = cudaMemcpyAsync(c->d_ent, host_ent, sizeof(int4) * c->ent_n, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "entry table upload");
+      c->ent_model = model;
+      c->ent_dim = dim;
+    }
+    const int nent = c->ent_n;
     ProfScope ps(c, JNE_KERNEL_ACCUM_FP64, st);
     e = jne_launch_accum_f64(a, c->d_ent, nent, c->sms, st);
   } else {
+    // per-chunk time means, exact (integer sums) then rounded once
+    const int nch = (steps + a.chunk - 1) / a.chunk;
+    if (c->ctab_steps != steps || c->ctab_chunk != a.chunk) {
+    int rc = ensure(c, &c->d_ctab, &c->ctab_cap, (size_t)nch, "chunk table");
+    if (rc) return rc;
+    c->h_ctab.resize(nch);
+    const long double T = steps;
+    for (int ch = 0; ch < nch; ch++) {
+      const long long c0 = (long long)ch * a.chunk, lc = std::min<long long>(a.chunk, steps - c0);
+      // columns i = c0 .. c0+lc-1 carry y = (i+1)/T
+      const long double s1 = (long double)lc * (2.0L * c0 + lc + 1.0L) / 2.0L;
+      auto sq = [](long double n) { return n * (n + 1.0L) * (2.0L * n + 1.0L) / 6.0L; };
+      const long double s2 = sq((long double)(c0 + lc)) - sq((long double)c0);
+      c->h_ctab[ch] = {(double)(s1 / (T * lc)), (double)(s2 / (T * T * lc)), (double)lc, 1.0 / (double)lc};
+    }
+    e = cudaMemcpyAsync(c->d_ctab, c->h_ctab.data(), sizeof(jne_chunk_time) * nch, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "chunk table upload");
+    c->ctab_steps = steps;
+    c->ctab_chunk = a.chunk;
+    }
+    a.chunk_tab = c->d_ctab;
     ProfScope ps(c, JNE_KERNEL_ACCUM_MIXED, st);
     e = jne_launch_accum_mixed(a, c->sms, st);
   }
@@ -272,6 +312,7 @@ void jne_close(jne_context* c) {
   cudaFree(c->d_ext);
   cudaFree(c->d_words);
   cudaFree(c->d_ent);
+  cudaFree(c->d_ctab);
   cudaFree(c->d_status);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -281,7 +322,8 @@ const char* jne_last_error(const jne_context* c) { return c ? c->err.c_str() : k
 
 int jne_set_chunk(jne_context* c, int chunk) {
   if (!c) return JNE_ERR_ARG;
-  if (chunk < 32 || chunk % 32 != 0 || chunk > (1 << 20)) return fail(c, JNE_ERR_ARG, "chunk must be a multiple of 32");
+  if (chunk != 0 && (chunk < 32 || chunk % 32 != 0 || chunk > (1 << 20)))
+    return fail(c, JNE_ERR_ARG, "chunk must be 0 (adaptive) or a multiple of 32");
   c->chunk = chunk;
   return JNE_OK;
 }

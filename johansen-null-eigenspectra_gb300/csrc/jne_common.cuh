@@ -20,44 +20,85 @@
 // for every model (johansen_statistics.rs:59-78) -- all five models see the same
 // path for a given seed.
 // ---------------------------------------------------------------------------
+// Round keys of the Philox4x32-10 key schedule (key bumped by the Weyl
+// constants between rounds).  They depend only on the stream key, so a kernel
+// computes them once.
+struct jne_round_keys {
+  uint32_t k0[10], k1[10];
+};
+
+__host__ __device__ __forceinline__ jne_round_keys jne_make_round_keys(uint32_t k0, uint32_t k1) {
+  jne_round_keys rk;
+  for (int r = 0; r < 10; r++) {
+    rk.k0[r] = k0 + (uint32_t)r * 0x9E3779B9u;
+    rk.k1[r] = k1 + (uint32_t)r * 0xBB67AE85u;
+  }
+  return rk;
+}
+
+// Ten rounds of the multiply/xor bijection; each 32x32->64 product yields both
+// halves at once.
 __device__ __forceinline__ void jne_philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                                  uint32_t k0, uint32_t k1, uint32_t out[4]) {
+                                                  const jne_round_keys& rk, uint32_t out[4]) {
 #pragma unroll
   for (int r = 0; r < 10; r++) {
-    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
-    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
+    const unsigned long long p0 = (unsigned long long)c0 * 0xD2511F53ull;
+    const unsigned long long p1 = (unsigned long long)c2 * 0xCD9E8D57ull;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ rk.k0[r];
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ rk.k1[r];
+    c1 = (uint32_t)p1;
+    c3 = (uint32_t)p0;
+    c0 = n0;
+    c2 = n2;
   }
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-// u in (0,1): the top 24 bits of a word plus half an ulp (exact in float).
+// u in (0,1): the top 23 bits m of a word, u = (m + 1/2) 2^-23, built in the
+// mantissa of a float in [1, 2) and shifted down (both steps exact).
 __device__ __forceinline__ float jne_u01(uint32_t x) {
-  return __fmaf_rn((float)(x >> 8), 5.9604644775390625e-08f, 2.98023223876953125e-08f);
+  return __fsub_rn(__uint_as_float(0x3F800000u | (x >> 9)), 0.99999994039535522f);
 }
 
-// Box-Muller pair: r = sqrt(-2 ln u(a)), theta = 2 pi u(b) - pi.  The hardware
-// approximations of log2/sin/cos are used; every rounding step is an explicit
-// _rn intrinsic so no caller can fuse it into a different FMA, which keeps the
-// generated values identical in every kernel that draws them.
+// Documented PTX approximations (single hardware instructions, so every kernel
+// that draws a value computes it the same way).
+__device__ __forceinline__ float jne_lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float jne_sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float jne_sin_approx(float x) {
+  float y;
+  asm("sin.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float jne_cos_approx(float x) {
+  float y;
+  asm("cos.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Box-Muller pair: r = sqrt(-2 ln u(a)), theta = 2 pi u(b) - pi, z = r (cos, sin).
+// Explicit _rn arithmetic keeps any caller from fusing a step into a different
+// FMA, so the values are identical in every kernel that draws them.
 __device__ __forceinline__ void jne_box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
-  const float l2 = __log2f(jne_u01(a));                        // log2(u) < 0
-  const float r = __fsqrt_rn(__fmul_rn(-1.3862943611198906f, l2));  // -2 ln 2 * log2(u)
+  const float l2 = jne_lg2_approx(jne_u01(a));                          // log2(u) < 0
+  const float r = jne_sqrt_approx(__fmul_rn(-1.3862943611198906f, l2));  // -2 ln 2 * log2(u)
   const float th = __fmaf_rn(jne_u01(b), 6.2831853071795865f, -3.1415926535897932f);
-  float s, c;
-  __sincosf(th, &s, &c);
-  z0 = __fmul_rn(r, c);
-  z1 = __fmul_rn(r, s);
+  z0 = __fmul_rn(r, jne_cos_approx(th));
+  z1 = __fmul_rn(r, jne_sin_approx(th));
 }
 
 // The four normals of quad j (features 4j..4j+3) of step s.
-__device__ __forceinline__ void jne_normal_quad(uint32_t s, uint32_t j, uint32_t seed, uint32_t k0, uint32_t k1,
+__device__ __forceinline__ void jne_normal_quad(uint32_t s, uint32_t j, uint32_t seed, const jne_round_keys& rk,
                                                 float z[4]) {
   uint32_t w[4];
-  jne_philox4x32_10(s, j, seed, 0u, k0, k1, w);
+  jne_philox4x32_10(s, j, seed, 0u, rk, w);
   jne_box_muller(w[0], w[1], z[0], z[1]);
   jne_box_muller(w[2], w[3], z[2], z[3]);
 }
@@ -91,12 +132,19 @@ __host__ __device__ __forceinline__ int jne_slot_Nzy(int a, int d) { return d * 
 __host__ __device__ __forceinline__ int jne_slot_Nzyy(int a, int d) { return d * (d + 1) / 2 + 5 * d + d * d + a; }
 __host__ __device__ __forceinline__ int jne_record_slots(int d) { return d * (d + 1) / 2 + 6 * d + d * d; }
 
+// Per-chunk time constants of the mixed kernel: mean of y and of y^2 over the
+// chunk's columns, its step count and the reciprocal.
+struct jne_chunk_time {
+  double ybar, y2bar, lc, inv_lc;
+};
+
 // Argument block of one accumulation launch: runs [0, n_runs) of one
 // (model, dim, steps) request; run r uses seed seed_first + r.
 struct jne_accum_args {
   int model, dim, steps, n_runs;
   uint32_t seed_first, key0, key1;
   int chunk;                 // mixed kernel: steps per FP32 chunk (multiple of 32)
+  const jne_chunk_time* chunk_tab;  // mixed kernel, one entry per chunk
   const double* ext;         // explicit increments [run][step][dim] (already scaled), or null
   double ext_inv_scale;      // mixed kernel: z = dB * ext_inv_scale when reading ext
   double* mom;               // moment records, SoA

@@ -1,0 +1,449 @@
+// jne_dat.cpp -- EIGENVALS_V6 storage, the simulation driver with resume, and
+// the percentile analyzer: the host side around the GPU path.
+//
+// Format (DATA_FORMAT.md, writer.rs:56-62, 242-249, 262-290):
+//   header  "EIGENVALS_V6" | u8 model | u8 dim | u32 steps (LE)           18 bytes
+//   record  ULEB128 u32 seed | u8 count | count x f64 (LE)
+//   trailer "EOF_MARK" | u64 record count (LE) | u8 eigenvalues per record  17 bytes
+#include <sys/stat.h>
+#include <sys/types.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/jne.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int dat_fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+const char kMagic[12] = {'E', 'I', 'G', 'E', 'N', 'V', 'A', 'L', 'S', '_', 'V', '6'};
+const char kEof[8] = {'E', 'O', 'F', '_', 'M', 'A', 'R', 'K'};
+constexpr size_t kHeader = 18, kTrailer = 17;
+
+// uleb128.rs:68-87
+size_t uleb_encode(uint32_t v, unsigned char* out) {
+  size_t n = 0;
+  do {
+    unsigned char b = v & 0x7F;
+    v >>= 7;
+    if (v) b |= 0x80;
+    out[n++] = b;
+  } while (v);
+  return n;
+}
+
+// uleb128.rs:102-137: 0 on success, -1 incomplete, -2 too long, -3 too large
+int uleb_decode(const unsigned char* p, size_t avail, uint32_t* v, size_t* used) {
+  uint32_t r = 0;
+  int shift = 0;
+  for (size_t i = 0; i < avail; i++) {
+    if (i + 1 > 5) return -2;
+    const uint32_t bits = p[i] & 0x7F;
+    if (shift == 28 && bits > 0x0F) return -3;
+    r |= bits << shift;
+    shift += 7;
+    if (!(p[i] & 0x80)) {
+      *v = r;
+      *used = i + 1;
+      return 0;
+    }
+  }
+  return -1;
+}
+
+void put_u32(unsigned char* p, uint32_t v) {
+  for (int i = 0; i < 4; i++) p[i] = (unsigned char)(v >> (8 * i));
+}
+void put_u64(unsigned char* p, uint64_t v) {
+  for (int i = 0; i < 8; i++) p[i] = (unsigned char)(v >> (8 * i));
+}
+uint32_t get_u32(const unsigned char* p) {
+  uint32_t v = 0;
+  for (int i = 3; i >= 0; i--) v = (v << 8) | p[i];
+  return v;
+}
+uint64_t get_u64(const unsigned char* p) {
+  uint64_t v = 0;
+  for (int i = 7; i >= 0; i--) v = (v << 8) | p[i];
+  return v;
+}
+void put_f64(unsigned char* p, double x) {
+  uint64_t u;
+  std::memcpy(&u, &x, 8);
+  put_u64(p, u);
+}
+double get_f64(const unsigned char* p) {
+  const uint64_t u = get_u64(p);
+  double x;
+  std::memcpy(&x, &u, 8);
+  return x;
+}
+
+bool file_exists(const char* path) {
+  struct stat st;
+  return stat(path, &st) == 0;
+}
+
+int read_file(const char* path, std::vector<unsigned char>* buf) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return dat_fail(JNE_ERR_IO, std::string(path) + ": " + std::strerror(errno));
+  std::fseek(f, 0, SEEK_END);
+  const long len = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  buf->resize(len > 0 ? (size_t)len : 0);
+  const size_t got = buf->empty() ? 0 : std::fread(buf->data(), 1, buf->size(), f);
+  std::fclose(f);
+  if (got != buf->size()) return dat_fail(JNE_ERR_IO, std::string(path) + ": short read");
+  return JNE_OK;
+}
+
+struct Parsed {
+  int model = 0, dim = 0, k = 0;
+  uint32_t steps = 0;
+  std::vector<uint32_t> seeds;
+  std::vector<double> eigs;
+};
+
+// reader.rs:23-216.  Fast path when the EOF trailer is present, scan otherwise.
+int parse(const std::vector<unsigned char>& b, Parsed* out, bool want_records) {
+  if (b.size() < 12 || std::memcmp(b.data(), kMagic, 12) != 0)
+    return dat_fail(JNE_ERR_FORMAT, "File format error: magic header mismatch");
+  if (b.size() < kHeader) return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
+  out->model = b[12];
+  out->dim = b[13];
+  out->steps = get_u32(&b[14]);
+  out->k = 0;
+  if (b.size() < kHeader + kTrailer) return JNE_OK;  // header only
+  const size_t n = b.size();
+  size_t pos = kHeader;
+  if (std::memcmp(&b[n - kTrailer], kEof, 8) == 0) {
+    const uint64_t total = get_u64(&b[n - 9]);
+    const int per = b[n - 1];
+    for (uint64_t r = 0; r < total; r++) {
+      uint32_t seed;
+      size_t used;
+      if (uleb_decode(&b[pos], n - kTrailer - pos, &seed, &used) != 0)
+        return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
+      pos += used;
+      if (pos >= n) return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
+      const int cnt = b[pos++];
+      if (cnt == 0) return dat_fail(JNE_ERR_FORMAT, "Invalid eigenvalue count: cannot be zero");
+      if (cnt != per)
+        return dat_fail(JNE_ERR_FORMAT, "Eigenvalue count mismatch: expected " + std::to_string(per) + ", actual " +
+                                            std::to_string(cnt));
+      if (pos + 8 * (size_t)cnt > n) return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
+      if (want_records) {
+        out->seeds.push_back(seed);
+        for (int j = 0; j < cnt; j++) out->eigs.push_back(get_f64(&b[pos + 8 * j]));
+      } else {
+        out->seeds.push_back(seed);
+      }
+      pos += 8 * (size_t)cnt;
+    }
+    out->k = per;
+    return JNE_OK;
+  }
+  // scan read (files without a trailer: interrupted runs)
+  int k = -1;
+  while (pos < n) {
+    uint32_t seed;
+    size_t used;
+    if (uleb_decode(&b[pos], n - pos, &seed, &used) != 0) break;
+    if (pos + used >= n) break;
+    const int cnt = b[pos + used];
+    if (cnt == 0) break;  // zero count: pre-allocated blank space or a trailer
+    if (pos + used + 1 + 8 * (size_t)cnt > n) break;  // incomplete record
+    if (k >= 0 && cnt != k)
+      return dat_fail(JNE_ERR_FORMAT, "Eigenvalue count mismatch: expected " + std::to_string(k) + ", actual " +
+                                          std::to_string(cnt));
+    k = cnt;
+    pos += used + 1;
+    out->seeds.push_back(seed);
+    if (want_records)
+      for (int j = 0; j < cnt; j++) out->eigs.push_back(get_f64(&b[pos + 8 * j]));
+    pos += 8 * (size_t)cnt;
+  }
+  out->k = k < 0 ? 0 : k;
+  return JNE_OK;
+}
+
+int write_header(FILE* f, int model, int dim, uint32_t steps) {
+  unsigned char h[kHeader];
+  std::memcpy(h, kMagic, 12);
+  h[12] = (unsigned char)model;
+  h[13] = (unsigned char)dim;
+  put_u32(h + 14, steps);
+  return std::fwrite(h, 1, kHeader, f) == kHeader ? JNE_OK : dat_fail(JNE_ERR_IO, "header write failed");
+}
+
+int mkdirs(const std::string& dir) {
+  if (dir.empty()) return JNE_OK;
+  std::string cur;
+  for (size_t i = 0; i <= dir.size(); i++) {
+    if (i == dir.size() || dir[i] == '/') {
+      if (!cur.empty() && mkdir(cur.c_str(), 0777) != 0 && errno != EEXIST)
+        return dat_fail(JNE_ERR_IO, "Failed to create data directory '" + cur + "': " + std::strerror(errno));
+    }
+    if (i < dir.size()) cur.push_back(dir[i]);
+  }
+  return JNE_OK;
+}
+
+}  // namespace
+
+struct jne_dat_writer {
+  FILE* f = nullptr;
+  int64_t count = 0;
+  int per_run = -1;
+  int model = 0, dim = 0;
+  uint32_t steps = 0;
+  std::vector<char> buf;
+  std::vector<unsigned char> rec;
+};
+
+extern "C" {
+
+const char* jne_dat_last_error(void) { return g_err.c_str(); }
+
+int jne_dat_open(const char* path, int model, int dim, uint32_t steps, jne_dat_writer** out, int64_t* existing) {
+  if (!path || !out) return dat_fail(JNE_ERR_ARG, "null argument");
+  if (model < 0 || model > 255 || dim < 0 || dim > 255) return dat_fail(JNE_ERR_ARG, "model and dim must fit u8");
+  *out = nullptr;
+  if (existing) *existing = 0;
+  jne_dat_writer* w = new jne_dat_writer();
+  w->model = model;
+  w->dim = dim;
+  w->steps = steps;
+  w->buf.resize(2u << 20);  // WRITE_BUFFER_CAPACITY, config.rs:9
+  bool fresh = !file_exists(path);
+  if (!fresh) {
+    std::vector<unsigned char> b;
+    Parsed p;
+    int rc = read_file(path, &b);
+    if (rc == JNE_OK) rc = parse(b, &p, false);
+    if (rc == JNE_OK) {
+      const char* what = nullptr;
+      int have = 0, want = 0;
+      if (p.model != model) { what = "Model"; have = p.model; want = model; }
+      else if (p.dim != dim) { what = "Dimension"; have = p.dim; want = dim; }
+      if (what) {
+        delete w;
+        return dat_fail(JNE_ERR_FORMAT, std::string(what) + " mismatch: file has " +
+                                            (what[0] == 'M' ? "model " : "dim ") + std::to_string(have) +
+                                            ", expected " + std::to_string(want));
+      }
+      if (p.steps != steps) {
+        delete w;
+        return dat_fail(JNE_ERR_FORMAT, "Steps mismatch: file has steps " + std::to_string(p.steps) +
+                                            ", expected " + std::to_string(steps));
+      }
+      w->count = (int64_t)p.seeds.size();
+      if (!p.seeds.empty()) w->per_run = p.k;
+    } else if (g_err.find("magic header mismatch") != std::string::npos) {
+      std::remove(path);  // incompatible format: recreate (writer.rs:116-150)
+      fresh = true;
+    }
+    if (!fresh) {  // strip a complete trailer so appends continue the record stream (writer.rs:181-203)
+      if (b.size() >= kHeader + kTrailer && std::memcmp(&b[b.size() - kTrailer], kEof, 8) == 0) {
+        if (truncate(path, (off_t)(b.size() - kTrailer)) != 0) {
+          delete w;
+          return dat_fail(JNE_ERR_IO, std::string("truncate: ") + std::strerror(errno));
+        }
+      }
+      w->f = std::fopen(path, "ab");
+    }
+  }
+  if (fresh) {
+    w->f = std::fopen(path, "wb");
+    if (w->f && write_header(w->f, model, dim, steps) != JNE_OK) {
+      std::fclose(w->f);
+      w->f = nullptr;
+    }
+  }
+  if (!w->f) {
+    delete w;
+    return dat_fail(JNE_ERR_IO, std::string(path) + ": " + std::strerror(errno));
+  }
+  std::setvbuf(w->f, w->buf.data(), _IOFBF, w->buf.size());
+  if (existing) *existing = w->count;
+  *out = w;
+  return JNE_OK;
+}
+
+int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs, int64_t n, int k) {
+  if (!w || (n > 0 && (!seeds || !eigs)) || n < 0) return dat_fail(JNE_ERR_ARG, "null argument");
+  if (k > 255)
+    return dat_fail(JNE_ERR_FORMAT, "Too many eigenvalues: " + std::to_string(k) + " exceeds maximum of 255");
+  if (k < 0) return dat_fail(JNE_ERR_ARG, "negative eigenvalue count");
+  if (n == 0) return JNE_OK;
+  if (w->per_run < 0) w->per_run = k;
+  if (k != w->per_run)
+    return dat_fail(JNE_ERR_FORMAT, "Eigenvalue count mismatch: expected " + std::to_string(w->per_run) +
+                                        ", actual " + std::to_string(k) + " (model " + std::to_string(w->model) +
+                                        ", dim " + std::to_string(w->dim) + ", steps " + std::to_string(w->steps) +
+                                        ")");
+  w->rec.resize(5 + 1 + 8 * (size_t)k);
+  for (int64_t r = 0; r < n; r++) {
+    size_t len = uleb_encode(seeds[r], w->rec.data());
+    w->rec[len++] = (unsigned char)k;
+    for (int j = 0; j < k; j++) put_f64(&w->rec[len + 8 * j], eigs[(size_t)r * k + j]);
+    len += 8 * (size_t)k;
+    if (std::fwrite(w->rec.data(), 1, len, w->f) != len) return dat_fail(JNE_ERR_IO, "record write failed");
+    w->count++;
+  }
+  return JNE_OK;
+}
+
+int jne_dat_finish(jne_dat_writer* w) {
+  if (!w) return dat_fail(JNE_ERR_ARG, "null writer");
+  unsigned char t[kTrailer];
+  std::memcpy(t, kEof, 8);
+  put_u64(t + 8, (uint64_t)w->count);
+  t[16] = (unsigned char)(w->per_run < 0 ? 0 : w->per_run);
+  int rc = std::fwrite(t, 1, kTrailer, w->f) == kTrailer ? JNE_OK : dat_fail(JNE_ERR_IO, "trailer write failed");
+  if (std::fclose(w->f) != 0 && rc == JNE_OK) rc = dat_fail(JNE_ERR_IO, "close failed");
+  delete w;
+  return rc;
+}
+
+void jne_dat_abandon(jne_dat_writer* w) {
+  if (!w) return;
+  std::fclose(w->f);
+  delete w;
+}
+
+int jne_dat_read(const char* path, int* model, int* dim, uint32_t* steps, int64_t* n, int* k, uint32_t* seeds,
+                 double* eigs, int64_t cap) {
+  if (!path) return dat_fail(JNE_ERR_ARG, "null path");
+  std::vector<unsigned char> b;
+  int rc = read_file(path, &b);
+  if (rc) return rc;
+  Parsed p;
+  const bool want = seeds && eigs;
+  if ((rc = parse(b, &p, want))) return rc;
+  if (model) *model = p.model;
+  if (dim) *dim = p.dim;
+  if (steps) *steps = p.steps;
+  if (n) *n = (int64_t)p.seeds.size();
+  if (k) *k = p.k;
+  if (want) {
+    if (cap < (int64_t)p.seeds.size()) return dat_fail(JNE_ERR_ARG, "buffer too small");
+    std::copy(p.seeds.begin(), p.seeds.end(), seeds);
+    std::copy(p.eigs.begin(), p.eigs.end(), eigs);
+  }
+  return JNE_OK;
+}
+
+int jne_simulation_filename(const char* data_dir, int model, int dim, int steps, char* buf, size_t cap) {
+  if (!buf || cap == 0) return dat_fail(JNE_ERR_ARG, "null buffer");
+  const std::string dir = data_dir && *data_dir ? data_dir : "data";
+  const std::string name = dir + "/eigenvalues_model" + std::to_string(model) + "_dim" + std::to_string(dim) +
+                           "_steps" + std::to_string(steps) + ".dat";
+  if (name.size() + 1 > cap) return dat_fail(JNE_ERR_ARG, "buffer too small");
+  std::memcpy(buf, name.c_str(), name.size() + 1);
+  return JNE_OK;
+}
+
+int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int dim, int steps, int64_t num_runs,
+                       int precision, uint64_t base_seed, int quiet) {
+  if (!ctx) return dat_fail(JNE_ERR_ARG, "null context");
+  if (jne_eigen_count(model, dim) < 0 || dim > JNE_MAX_DIM || steps < 1 || num_runs < 0 || num_runs > 0xFFFFFFFFll)
+    return dat_fail(JNE_ERR_ARG, "bad simulation parameters");
+  const std::string dir = data_dir && *data_dir ? data_dir : "data";
+  int rc = mkdirs(dir);
+  if (rc) return rc;
+  char path[4096];
+  if ((rc = jne_simulation_filename(dir.c_str(), model, dim, steps, path, sizeof path))) return rc;
+
+  // progress (progress.rs:11-53): seeds already in the file; other parameters -> start over
+  std::unordered_set<uint32_t> done;
+  if (file_exists(path)) {
+    std::vector<unsigned char> b;
+    Parsed p;
+    if (read_file(path, &b) == JNE_OK && parse(b, &p, false) == JNE_OK) {
+      if (p.model != model || p.dim != dim || p.steps != (uint32_t)steps) {
+        if (!quiet) std::printf("WARNING: Existing file has incompatible parameters; recreating %s\n", path);
+        std::remove(path);
+      } else {
+        done.insert(p.seeds.begin(), p.seeds.end());
+      }
+    }
+  }
+  std::vector<uint32_t> remaining;  // progress.rs:56-61, seeds 1..=num_runs
+  for (int64_t s = 1; s <= num_runs; s++)
+    if (!done.count((uint32_t)s)) remaining.push_back((uint32_t)s);
+  if (remaining.empty()) {
+    if (!quiet) std::printf("SUCCESS: calculation for this model already completed, skipping\n");
+    return JNE_OK;
+  }
+  if (!quiet)
+    std::printf("Remaining %zu calculations to complete (model %d, dim %d, steps %d)\n", remaining.size(), model,
+                dim, steps);
+  jne_dat_writer* w = nullptr;
+  if ((rc = jne_dat_open(path, model, dim, (uint32_t)steps, &w, nullptr))) return rc;
+  const int k = jne_eigen_count(model, dim);
+  const int64_t batch = 1 << 18;
+  std::vector<double> eig;
+  for (size_t i = 0; i < remaining.size();) {
+    // largest contiguous seed range starting at remaining[i], capped at `batch`
+    size_t j = i + 1;
+    while (j < remaining.size() && remaining[j] == remaining[j - 1] + 1 && (int64_t)(j - i) < batch) j++;
+    const int64_t n = (int64_t)(j - i);
+    eig.resize((size_t)n * k);
+    rc = jne_eigs_seeded(ctx, model, dim, steps, base_seed, remaining[i], n, precision, eig.data());
+    if (rc) {
+      g_err = jne_last_error(ctx);
+      jne_dat_abandon(w);  // keep what was written; a rerun resumes
+      return rc;
+    }
+    if ((rc = jne_dat_append(w, &remaining[i], eig.data(), n, k))) {
+      jne_dat_abandon(w);
+      return rc;
+    }
+    i = j;
+  }
+  return jne_dat_finish(w);
+}
+
+int jne_percentiles(const double* eigs, int64_t n, int k, int stat, const double* ps, int np, double* out) {
+  if ((n > 0 && !eigs) || (np > 0 && (!ps || !out)) || k < 1 || n < 0 || (stat != 0 && stat != 1))
+    return dat_fail(JNE_ERR_ARG, "bad percentile arguments");
+  std::vector<double> v((size_t)n);
+  for (int64_t r = 0; r < n; r++) {  // Sum / Max aggregators, simulation_analyzers.rs:26-39
+    const double* e = eigs + (size_t)r * k;
+    double a = stat == 0 ? 0.0 : -1.7976931348623157e308;
+    for (int j = 0; j < k; j++) a = stat == 0 ? a + e[j] : std::max(a, e[j]);
+    v[(size_t)r] = a;
+  }
+  std::sort(v.begin(), v.end());
+  for (int i = 0; i < np; i++) {  // simulation_analyzers.rs:4-18
+    if (n == 0) {
+      out[i] = NAN;
+      continue;
+    }
+    const double rank = ps[i] * (double)(n - 1);
+    const int64_t lo = (int64_t)std::floor(rank), hi = (int64_t)std::ceil(rank);
+    if (lo == hi) {
+      out[i] = v[(size_t)lo];
+    } else {
+      const double wgt = rank - (double)lo;
+      out[i] = v[(size_t)lo] * (1.0 - wgt) + v[(size_t)hi] * wgt;
+    }
+  }
+  return JNE_OK;
+}
+
+}  // extern "C"

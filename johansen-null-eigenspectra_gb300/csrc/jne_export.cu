@@ -13,16 +13,17 @@ __global__ void k_export(int dim, int steps, int n_runs, uint32_t seed_first, ui
   const int run = (int)(idx / steps), i = (int)(idx % steps);
   const int nq = (dim + 3) >> 2;
   const uint32_t seed = seed_first + (uint32_t)run;
+  const jne_round_keys rk = jne_make_round_keys(key0, key1);
   for (int j = 0; j < nq; j++) {
     if (words) {
       uint32_t w[4];
-      jne_philox4x32_10((uint32_t)(i + 1), (uint32_t)j, seed, 0u, key0, key1, w);
+      jne_philox4x32_10((uint32_t)(i + 1), (uint32_t)j, seed, 0u, rk, w);
       uint32_t* dst = words + ((size_t)idx * nq + j) * 4;
       dst[0] = w[0]; dst[1] = w[1]; dst[2] = w[2]; dst[3] = w[3];
     }
     if (out) {
       float z[4];
-      jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, key0, key1, z);
+      jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, rk, z);
       for (int e = 0; e < 4; e++) {
         const int f = 4 * j + e;
         if (f < dim) out[(size_t)idx * dim + f] = (double)z[e] * scale;

@@ -80,7 +80,8 @@ void jno_philox_words(uint64_t base_seed, int dim, uint32_t run_seed, int steps,
     }
 }
 
-static inline double jno_u01(uint32_t x) { return ((double)(x >> 8) + 0.5) * (1.0 / 16777216.0); }
+/* u in (0,1): the top 23 bits m of a word, u = (m + 1/2) 2^-23. */
+static inline double jno_u01(uint32_t x) { return ((double)(x >> 9) + 0.5) * (1.0 / 8388608.0); }
 
 /* Box-Muller on two words: z0 = r cos(theta), z1 = r sin(theta) with
  * r = sqrt(-2 ln u(a)), theta = 2 pi u(b) - pi. */

@@ -70,7 +70,7 @@ def philox_words(base_seed: int, dim: int, run_seed: int, steps: int) -> np.ndar
 def normals(base_seed: int, dim: int, run_seed: int, steps: int) -> np.ndarray:
     """Standard normals of one run, shape (steps, dim) (Box-Muller in float64)."""
     w = philox_words(base_seed, dim, run_seed, steps).astype(np.float64)
-    u = (np.floor(w / 256.0) + 0.5) / 16777216.0
+    u = (np.floor(w / 512.0) + 0.5) / 8388608.0  # top 23 bits + half an ulp
     r01 = np.sqrt(-2.0 * np.log(u[..., 0]))
     r23 = np.sqrt(-2.0 * np.log(u[..., 2]))
     t01 = 2.0 * np.pi * u[..., 1] - np.pi

@@ -1,0 +1,148 @@
+"""EIGENVALS_V6 storage and the percentile rule through the C ABI (host code, no
+GPU), checked byte for byte against the oracle's restatement of the format and
+against the assertions of the reference's append_writer_test.rs."""
+import os
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture
+def tmp(tmp_path):
+    return str(tmp_path)
+
+
+def test_bytes_match_format_restatement(jne, oracle, tmp):
+    path = os.path.join(tmp, "a.dat")
+    recs = [(1, [1.0, 2.0]), (300, [3.0, 4.0]), (16384, [5.5, -0.25]), (2**32 - 1, [7.0, 8.0])]
+    w = jne.DatWriter(path, 0, 2, 100)
+    for s, e in recs:
+        w.append_eigenvalues(s, e)
+    w.finish()
+    assert open(path, "rb").read() == oracle.dat_bytes(0, 2, 100, recs)
+
+
+def test_roundtrip_basic(jne, tmp):  # append_writer_test.rs:5-31
+    path = os.path.join(tmp, "basic.dat")
+    w = jne.DatWriter(path, 0, 2, 100)
+    w.append_eigenvalues(1, [1.0, 2.0])
+    w.append_eigenvalues(2, [3.0, 4.0])
+    w.finish()
+    recs, model, dim, steps = jne.read_dat(path)
+    assert (model, dim, steps) == (0, 2, 100)
+    assert [(s, list(e)) for s, e in recs] == [(1, [1.0, 2.0]), (2, [3.0, 4.0])]
+
+
+def test_incomplete_file_is_scanned(jne, oracle, tmp):  # append_writer_test.rs:66-93
+    path = os.path.join(tmp, "inc.dat")
+    w = jne.DatWriter(path, 2, 2, 150)
+    w.append_eigenvalues(1, [1.0, 2.0])
+    w.append_eigenvalues(2, [3.0, 4.0])
+    w.abandon()
+    recs, *_ = jne.read_dat(path)
+    assert [(s, list(e)) for s, e in recs] == [(1, [1.0, 2.0]), (2, [3.0, 4.0])]
+    # a record cut in the middle is dropped, as the reference's scan read does
+    with open(path, "ab") as f:
+        f.write(bytes([3, 2]) + b"\x00" * 11)
+    recs, *_ = jne.read_dat(path)
+    assert len(recs) == 2
+
+
+def test_large_dataset_and_resume_append(jne, tmp):  # append_writer_test.rs:95-123
+    path = os.path.join(tmp, "large.dat")
+    w = jne.DatWriter(path, 3, 2, 500)
+    seeds = np.arange(1, 1001)
+    w.append(seeds, np.stack([seeds * 0.1, seeds * 0.2], axis=1))
+    w.finish()
+    recs, *_ = jne.read_dat(path)
+    assert len(recs) == 1000 and recs[0][0] == 1 and list(recs[999][1]) == [100.0, 200.0]
+    # reopen: the trailer is stripped, records continue, a new trailer counts all
+    w = jne.DatWriter(path, 3, 2, 500)
+    assert w.existing == 1000
+    w.append([1001], np.array([[1.5, 2.5]]))
+    w.finish()
+    recs, *_ = jne.read_dat(path)
+    assert len(recs) == 1001 and recs[1000][0] == 1001
+    raw = open(path, "rb").read()
+    assert raw[-17:-9] == b"EOF_MARK" and int.from_bytes(raw[-9:-1], "little") == 1001 and raw[-1] == 2
+
+
+def test_eigenvalue_count_consistency(jne, tmp):  # append_writer_test.rs:125-144
+    w = jne.DatWriter(os.path.join(tmp, "c.dat"), 0, 2, 100)
+    w.append_eigenvalues(1, [1.0, 2.0])
+    with pytest.raises(jne.DatError) as ei:
+        w.append_eigenvalues(2, [3.0, 4.0, 5.0])
+    assert "Eigenvalue count mismatch" in str(ei.value)
+    w.abandon()
+
+
+def test_eigenvalue_count_limits(jne, tmp):  # append_writer_test.rs:146-197
+    w = jne.DatWriter(os.path.join(tmp, "o.dat"), 0, 255, 1000)
+    with pytest.raises(jne.DatError) as ei:
+        w.append_eigenvalues(1, list(range(300)))
+    assert "Too many eigenvalues" in str(ei.value) and "exceeds maximum of 255" in str(ei.value)
+    w.abandon()
+    path = os.path.join(tmp, "b.dat")
+    w = jne.DatWriter(path, 4, 255, 1000)
+    w.append_eigenvalues(1, [float(i) for i in range(255)])
+    w.finish()
+    recs, *_ = jne.read_dat(path)
+    assert len(recs) == 1 and len(recs[0][1]) == 255
+
+
+def test_parameter_validation(jne, tmp):  # append_writer_test.rs:199-227
+    path = os.path.join(tmp, "p.dat")
+    w = jne.DatWriter(path, 1, 3, 100)
+    w.append_eigenvalues(1, [1.0, 2.0, 3.0])
+    w.finish()
+    for args, text in (((2, 3, 100), "Model mismatch: file has model 1, expected 2"),
+                       ((1, 4, 100), "Dimension mismatch: file has dim 3, expected 4"),
+                       ((1, 3, 200), "Steps mismatch: file has steps 100, expected 200")):
+        with pytest.raises(jne.DatError) as ei:
+            jne.DatWriter(path, *args)
+        assert text in str(ei.value)
+    jne.DatWriter(path, 1, 3, 100).finish()
+
+
+def test_foreign_magic_is_recreated_and_unreadable_errors(jne, tmp):
+    path = os.path.join(tmp, "m.dat")
+    open(path, "wb").write(b"EIGENVALS_V5" + bytes(40))
+    with pytest.raises(jne.DatError) as ei:
+        jne.read_dat(path)
+    assert "magic header mismatch" in str(ei.value)
+    w = jne.DatWriter(path, 0, 1, 10)  # writer.rs:116-150: incompatible format -> recreate
+    assert w.existing == 0
+    w.append_eigenvalues(1, [1.0])
+    w.finish()
+    assert len(jne.read_dat(path)[0]) == 1
+    with pytest.raises(jne.DatError) as ei:
+        jne.read_dat(os.path.join(tmp, "missing.dat"))
+    assert ei.value.code == jne.JNE_ERR_IO
+
+
+def test_header_only_file(jne, oracle, tmp):
+    path = os.path.join(tmp, "h.dat")
+    open(path, "wb").write(oracle.dat_bytes(0, 1, 10, [], finished=False))
+    recs, model, dim, steps = jne.read_dat(path)
+    assert len(recs) == 0 and (model, dim, steps) == (0, 1, 10)
+
+
+def test_percentiles_match_rule(jne, oracle):
+    rng = np.random.default_rng(5)
+    eigs = np.sort(rng.gamma(2.0, 3.0, size=(501, 4)), axis=1)[:, ::-1]
+    ps = [0.01, 0.05, 0.1, 0.5, 0.9, 0.95, 0.99, 0.0, 1.0]
+    tr = jne.percentiles(eigs, "trace", ps)
+    mx = jne.percentiles(eigs, "maxeig", ps)
+    for p, a, b in zip(ps, tr, mx):
+        assert abs(a - oracle.percentile_value(np.sort(eigs.sum(1)), p)) < 1e-12
+        assert abs(b - oracle.percentile_value(np.sort(eigs.max(1)), p)) < 1e-12
+    assert np.isnan(jne.percentiles(np.zeros((0, 3)), "trace", [0.5])[0])
+
+
+def test_simulation_filenames(jne, tmp):  # filename_consistency.rs, simulation_test.rs:47-78
+    for m in range(5):
+        sim = jne.EigenvalueSimulation(m, 3, 500, 1000, data_dir=os.path.join(tmp, "data"))
+        assert os.path.basename(sim.get_filename(m)) == f"eigenvalues_model{m}_dim3_steps500.dat"
+    a = jne.EigenvalueSimulation(0, 5, 999, 100, data_dir=tmp).get_filename()
+    b = jne.EigenvalueSimulation(0, 5, 999, 500, data_dir=tmp).get_filename()
+    assert a == b and os.path.basename(a) == "eigenvalues_model0_dim5_steps999.dat"
