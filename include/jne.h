@@ -48,6 +48,9 @@ extern "C" {
 /* arithmetic of the Gram contraction */
 #define JNE_PREC_FP64 0  /* plain FP64 fused kernel */
 #define JNE_PREC_MIXED 1 /* split-TF32 tensor-core Grams, FP32 chunks, FP64 merge + solve */
+/* JNE_PREC_MIXED requests with fewer steps than this run the FP64 kernel: on
+ * such short paths the FP32 chunk part is most of every moment. */
+#define JNE_MIXED_MIN_STEPS 256
 
 #define JNE_MAX_DIM 12
 #define JNE_DEFAULT_BASE_SEED 0x4A4F48ull
@@ -68,7 +71,8 @@ void jne_close(jne_context* ctx);
 /* message of the last failed call on ctx (never null) */
 const char* jne_last_error(const jne_context* ctx);
 
-/* steps per FP32 chunk of the mixed kernel (multiple of 32; default 256) */
+/* Steps per FP32 chunk of the mixed kernel: a multiple of 32, or 0 (the
+ * default) for about steps/32 rounded down to a power of two in [32, 256]. */
 int jne_set_chunk(jne_context* ctx, int chunk);
 
 /* Eigenvalues of n_runs runs from explicit increments.  dB holds n_runs

@@ -173,9 +173,18 @@ int64_t batch_runs(const jne_context* c, int dim, int k_total) {
   return n;
 }
 
+// The kernel a request runs on.  Mixed-precision requests on paths shorter
+// than JNE_MIXED_MIN_STEPS use the FP64 kernel: with so few chunks the FP32
+// part is most of every moment (errors up to ~1e-4 at T = 16, dim 12), and
+// such paths are cheap in FP64 anyway.
+int kernel_precision(int precision, int steps) {
+  return (precision == JNE_PREC_MIXED && steps >= JNE_MIXED_MIN_STEPS) ? JNE_PREC_MIXED : JNE_PREC_FP64;
+}
+
 // Moments of runs [seed_first, seed_first + n) into c->d_mom (leading dim n).
 int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uint32_t key1, uint32_t seed_first,
                int n, int precision, const double* d_ext, cudaStream_t st) {
+  precision = kernel_precision(precision, steps);
   jne_accum_args a{};
   a.model = model;
   a.dim = dim;
@@ -365,7 +374,7 @@ int jne_eigs_from_increments(jne_context* c, int model, int dim, int steps, cons
   if (e != cudaSuccess) return cuda_fail(c, e, "increment upload");
   if ((rc = accumulate(c, model, dim, steps, 0, 0, 0, n_runs, precision, c->d_ext, st))) return rc;
   // FP64 walks the increments as given; the mixed kernel walks dB * sqrt(T)
-  const double zscale = precision == JNE_PREC_FP64 ? 1.0 : 1.0 / std::sqrt((double)steps);
+  const double zscale = kernel_precision(precision, steps) == JNE_PREC_FP64 ? 1.0 : 1.0 / std::sqrt((double)steps);
   if ((rc = finalize(c, model, dim, steps, n_runs, zscale, c->d_out, st))) return rc;
   e = cudaMemcpyAsync(out, c->d_out, sizeof(double) * n_runs * k, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "result download");

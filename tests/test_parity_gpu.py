@@ -3,12 +3,12 @@
 Tolerances (per run, max_j |got - ref| / max(max_j |ref|, floor)):
   plain FP64 kernel   1e-9, floor 0 (plain normwise-relative)
   mixed kernel        floor 1 (absolute for runs whose eigenvalues are all below
-                      1, see conftest.normwise_err) and a tolerance that depends on
-                      the path length (tol_mixed): 2e-6 from T = 1000 on; short
-                      paths have few chunks, so the FP32 centred part is a larger
-                      share of every moment.  At dim 12, T 10^4 the max-eigenvalue
-                      and trace errors against the FP64 kernel on identical seeds
-                      must stay <= 1e-6 (relative) for every run.
+                      1, see conftest.normwise_err): 2e-6 from T = 1000 on, 4e-6
+                      for 256 <= T < 1000 (few chunks: the FP32 centred part is a
+                      larger share of every moment); below T = 256 mixed requests
+                      run the FP64 kernel (JNE_MIXED_MIN_STEPS).  At dim 12, T 10^4
+                      the max-eigenvalue and trace errors against the FP64 kernel
+                      on identical seeds must stay <= 1e-6 (relative) every run.
 """
 import numpy as np
 import pytest
@@ -22,14 +22,13 @@ TOL_MIXED = 2e-6
 FLOOR = {0: 0.0, 1: 1.0}  # per precision
 
 
+MIXED_MIN_STEPS = 256  # JNE_MIXED_MIN_STEPS: shorter mixed requests run the FP64 kernel
+
+
 def tol_mixed(steps: int) -> float:
-    if steps >= 1000:
-        return 2e-6
-    if steps >= 256:
-        return 4e-6
-    if steps >= 64:
-        return 2e-5
-    return 2e-4
+    if steps < MIXED_MIN_STEPS:
+        return TOL_FP64
+    return 2e-6 if steps >= 1000 else 4e-6
 
 
 def tol(precision: int, steps: int) -> float:
@@ -89,7 +88,7 @@ def test_run_result_independent_of_batch_and_repeatable(engine, precision):
     assert np.array_equal(big, engine.eigs_seeded(3, 7, 777, 1, 40, precision=precision))
 
 
-@pytest.mark.parametrize("steps", [2, 3, 31, 32, 33, 63, 255, 257, 300])
+@pytest.mark.parametrize("steps", [2, 3, 31, 32, 33, 63, 255, 256, 257, 300, 513])
 def test_ragged_step_counts(engine, oracle, steps):
     for dim in (1, 2, 12):
         dB, _ = engine.export_increments(dim, steps, 5, 3)
@@ -108,6 +107,15 @@ def test_singular_s11_is_reported(engine, jne):
     with pytest.raises(jne.JneError) as ei:
         engine.eigs_seeded(0, 1, 1, 1, 2)
     assert ei.value.code == jne.JNE_ERR_NUMERIC
+
+
+def test_short_mixed_requests_run_fp64(engine):
+    for steps in (40, 255):
+        f = engine.eigs_seeded(2, 5, steps, 1, 6, precision=0)
+        assert np.array_equal(engine.eigs_seeded(2, 5, steps, 1, 6, precision=1), f)
+    f = engine.eigs_seeded(2, 5, 256, 1, 6, precision=0)
+    m = engine.eigs_seeded(2, 5, 256, 1, 6, precision=1)
+    assert not np.array_equal(m, f) and normwise_err(m, f, 1.0) < tol_mixed(256)
 
 
 def test_empty_batch(engine):
