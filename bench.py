@@ -200,6 +200,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         ev1.record(stream)
         barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1))
+    eng.sync()  # device status of the asynchronous calls
     prof = eng.profile_read(reset=True)
     eng.profile(False)
     runs_per_step = R * len(MODELS) * world
@@ -237,6 +238,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         eng.eigs_seeded_device(m, DIM, STEPS, seed0, Rf, outs[m].data_ptr(), precision=jne.PREC_FP64, stream=sptr)
     f1.record(stream)
     barrier()
+    eng.sync()
     fp64_ms = max_over_ranks(f0.elapsed_time(f1))
     fp64_value = Rf * len(MODELS) * world / (fp64_ms * 1e-3)
 

@@ -86,10 +86,17 @@ int jne_eigs_from_increments(jne_context* ctx, int model, int dim, int steps, co
 int jne_eigs_seeded(jne_context* ctx, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
                     int64_t n_runs, int precision, double* out);
 
-/* As jne_eigs_seeded, with out in device memory, enqueued on `stream` (a
- * cudaStream_t; null = the context's stream) and synchronised before return. */
+/* As jne_eigs_seeded, with out in device memory, enqueued asynchronously:
+ * work later enqueued on `stream` (a cudaStream_t; null = the context's
+ * stream) sees the results, and the call returns without waiting.  Consecutive
+ * calls overlap (the finalize of one batch runs beside the accumulation of the
+ * next).  Device-side errors (a non-SPD S11) are reported by jne_sync. */
 int jne_eigs_seeded_device(jne_context* ctx, int model, int dim, int steps, uint64_t base_seed,
                            uint32_t seed_first, int64_t n_runs, int precision, double* out_device, void* stream);
+
+/* Waits for all work of ctx and returns (then clears) the device status of the
+ * asynchronous calls since the last jne_sync. */
+int jne_sync(jne_context* ctx);
 
 /* Several models of one (dim, steps) pair from one pass over the paths (the
  * path of a seed does not depend on the model).  models[m] lists n_models

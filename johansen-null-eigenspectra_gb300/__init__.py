@@ -30,7 +30,7 @@ MAX_DIM = 12
 EXPORTS = (
     "jne_version", "jne_eigen_count", "jne_open", "jne_close", "jne_last_error", "jne_set_chunk",
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
-    "jne_export_increments", "jne_profile", "jne_profile_read",
+    "jne_export_increments", "jne_profile", "jne_profile_read", "jne_sync",
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
     "jne_simulation_filename", "jne_simulation_run", "jne_percentiles",
 )
@@ -132,6 +132,7 @@ def lib() -> ctypes.CDLL:
         L.jne_eigs_seeded_models.argtypes = [vp, ctypes.POINTER(c_int), c_int, c_int, c_int, c_u64, c_u32, c_i64,
                                              c_int, ctypes.POINTER(dp)]
         L.jne_export_increments.argtypes = [vp, c_int, c_int, c_u64, c_u32, c_int, dp, ctypes.POINTER(c_u32)]
+        L.jne_sync.argtypes = [vp]
         L.jne_profile.argtypes = [vp, c_int]
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
@@ -219,9 +220,14 @@ class Engine:
     def eigs_seeded_device(self, model: int, dim: int, steps: int, seed_first: int, n_runs: int, out_ptr: int,
                            precision: int = PREC_FP64, base_seed: int = DEFAULT_BASE_SEED,
                            stream: Optional[int] = None) -> None:
-        """Results into the device buffer at out_ptr (n_runs x k doubles)."""
+        """Results into the device buffer at out_ptr (n_runs x k doubles); asynchronous:
+        work later enqueued on `stream` sees them, and sync() reports device errors."""
         self._check(self._L.jne_eigs_seeded_device(self._h, int(model), dim, steps, base_seed, seed_first, n_runs,
                                                    precision, ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
+
+    def sync(self) -> None:
+        """Wait for all asynchronous work and raise on its device status (jne_sync)."""
+        self._check(self._L.jne_sync(self._h))
 
     def eigs_seeded_models(self, models: Sequence[int], dim: int, steps: int, seed_first: int, n_runs: int,
                            precision: int = PREC_FP64, base_seed: int = DEFAULT_BASE_SEED) -> Dict[int, np.ndarray]:

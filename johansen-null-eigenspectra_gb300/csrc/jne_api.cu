@@ -34,6 +34,13 @@ struct jne_context {
   size_t ent_cap = 0;
   unsigned int* d_status = nullptr;
   std::string err;
+  // asynchronous device path: two record buffers, finalize on a second stream
+  cudaStream_t fin_stream = nullptr;
+  cudaEvent_t ev_acc[2] = {nullptr, nullptr}, ev_fin[2] = {nullptr, nullptr};
+  bool fin_pending[2] = {false, false};
+  double* d_momb[2] = {nullptr, nullptr};
+  size_t momb_cap[2] = {0, 0};
+  unsigned long long batch_seq = 0;
   // per-kernel event timing (jne_profile)
   bool profiling = false;
   struct Timed {
@@ -183,7 +190,7 @@ int kernel_precision(int precision, int steps) {
 
 // Moments of runs [seed_first, seed_first + n) into c->d_mom (leading dim n).
 int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uint32_t key1, uint32_t seed_first,
-               int n, int precision, const double* d_ext, cudaStream_t st) {
+               int n, int precision, const double* d_ext, double* mom, cudaStream_t st) {
   precision = kernel_precision(precision, steps);
   jne_accum_args a{};
   a.model = model;
@@ -196,7 +203,7 @@ int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uin
   a.chunk = c->chunk ? c->chunk : adaptive_chunk(steps);
   a.ext = d_ext;
   a.ext_inv_scale = std::sqrt((double)steps);
-  a.mom = c->d_mom;
+  a.mom = mom;
   a.mom_ld = n;
   a.status = c->d_status;
   cudaError_t e;
@@ -243,7 +250,8 @@ int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uin
   return JNE_OK;
 }
 
-int finalize(jne_context* c, int model, int dim, int steps, int n, double zscale, double* d_out, cudaStream_t st) {
+int finalize(jne_context* c, int model, int dim, int steps, int n, double zscale, const double* mom, double* d_out,
+             cudaStream_t st) {
   jne_finalize_args f{};
   f.model = model;
   f.dim = dim;
@@ -251,7 +259,7 @@ int finalize(jne_context* c, int model, int dim, int steps, int n, double zscale
   f.n_runs = n;
   f.zscale = zscale;
   f.ts = time_sums(steps);
-  f.mom = c->d_mom;
+  f.mom = mom;
   f.mom_ld = n;
   f.out = d_out;
   f.status = c->d_status;
@@ -270,6 +278,13 @@ int check_common(jne_context* c, int model, int dim, int steps, int64_t n_runs, 
   if (precision != JNE_PREC_FP64 && precision != JNE_PREC_MIXED) return fail(c, JNE_ERR_ARG, "unknown precision");
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, JNE_ERR_CUDA, "cudaSetDevice failed");
   return JNE_OK;
+}
+
+// Waits for the asynchronous device path, so a synchronous call owns the status word.
+int drain(jne_context* c) {
+  cudaError_t e = cudaStreamSynchronize(c->fin_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? JNE_OK : cuda_fail(c, e, "drain");
 }
 
 int clear_status(jne_context* c, cudaStream_t st) {
@@ -300,6 +315,11 @@ int jne_open(int device, unsigned long long mem_budget_bytes, jne_context** out)
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->fin_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    e = cudaEventCreateWithFlags(&c->ev_acc[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fin[i], cudaEventDisableTiming);
+  }
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, sizeof(unsigned int));
   if (e != cudaSuccess) {
     jne_close(c);
@@ -313,6 +333,7 @@ int jne_open(int device, unsigned long long mem_budget_bytes, jne_context** out)
 void jne_close(jne_context* c) {
   if (!c) return;
   cudaSetDevice(c->device);
+  if (c->fin_stream) cudaStreamSynchronize(c->fin_stream);
   if (c->stream) cudaStreamSynchronize(c->stream);
   prof_flush(c);
   for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
@@ -323,6 +344,12 @@ void jne_close(jne_context* c) {
   cudaFree(c->d_ent);
   cudaFree(c->d_ctab);
   cudaFree(c->d_status);
+  for (int i = 0; i < 2; i++) {
+    cudaFree(c->d_momb[i]);
+    if (c->ev_acc[i]) cudaEventDestroy(c->ev_acc[i]);
+    if (c->ev_fin[i]) cudaEventDestroy(c->ev_fin[i]);
+  }
+  if (c->fin_stream) cudaStreamDestroy(c->fin_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -369,13 +396,14 @@ int jne_eigs_from_increments(jne_context* c, int model, int dim, int steps, cons
   if ((rc = ensure(c, &c->d_mom, &c->mom_cap, (size_t)n_runs * jne_record_slots(dim), "moment buffer"))) return rc;
   if ((rc = ensure(c, &c->d_out, &c->out_cap, (size_t)n_runs * k, "output buffer"))) return rc;
   cudaStream_t st = c->stream;
+  if ((rc = drain(c))) return rc;
   if ((rc = clear_status(c, st))) return rc;
   cudaError_t e = cudaMemcpyAsync(c->d_ext, dB, sizeof(double) * n_ext, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "increment upload");
-  if ((rc = accumulate(c, model, dim, steps, 0, 0, 0, n_runs, precision, c->d_ext, st))) return rc;
+  if ((rc = accumulate(c, model, dim, steps, 0, 0, 0, n_runs, precision, c->d_ext, c->d_mom, st))) return rc;
   // FP64 walks the increments as given; the mixed kernel walks dB * sqrt(T)
   const double zscale = kernel_precision(precision, steps) == JNE_PREC_FP64 ? 1.0 : 1.0 / std::sqrt((double)steps);
-  if ((rc = finalize(c, model, dim, steps, n_runs, zscale, c->d_out, st))) return rc;
+  if ((rc = finalize(c, model, dim, steps, n_runs, zscale, c->d_mom, c->d_out, st))) return rc;
   e = cudaMemcpyAsync(out, c->d_out, sizeof(double) * n_runs * k, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "result download");
   return check_status(c);
@@ -399,20 +427,22 @@ int jne_eigs_seeded_models(jne_context* c, const int* models, int n_models, int 
   const int acc_model = (n_models == 1) ? models[0] : -1;
   const double zscale = 1.0 / std::sqrt((double)steps);
   cudaStream_t st = c->stream;
-  int rc = clear_status(c, st);
+  int rc = drain(c);
   if (rc) return rc;
+  if ((rc = clear_status(c, st))) return rc;
   const int64_t per = batch_runs(c, dim, k_total);
   if (per < 1) return fail(c, JNE_ERR_BUDGET, "budget too small for one run");
   for (int64_t done = 0; done < n_runs; done += per) {
     const int n = (int)std::min<int64_t>(per, n_runs - done);
     if ((rc = ensure(c, &c->d_mom, &c->mom_cap, (size_t)n * jne_record_slots(dim), "moment buffer"))) return rc;
     if ((rc = ensure(c, &c->d_out, &c->out_cap, (size_t)n * k_total, "output buffer"))) return rc;
-    if ((rc = accumulate(c, acc_model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr, st)))
+    if ((rc = accumulate(c, acc_model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
+                         c->d_mom, st)))
       return rc;
     size_t off = 0;
     for (int m = 0; m < n_models; m++) {
       const int k = jne_eigen_count(models[m], dim);
-      if ((rc = finalize(c, models[m], dim, steps, n, zscale, c->d_out + off, st))) return rc;
+      if ((rc = finalize(c, models[m], dim, steps, n, zscale, c->d_mom, c->d_out + off, st))) return rc;
       cudaError_t e = cudaMemcpyAsync(outs[m] + (size_t)done * k, c->d_out + off, sizeof(double) * n * k,
                                       cudaMemcpyDeviceToHost, st);
       if (e != cudaSuccess) return cuda_fail(c, e, "result download");
@@ -439,21 +469,48 @@ int jne_eigs_seeded_device(jne_context* c, int model, int dim, int steps, uint64
   uint32_t k0, k1;
   stream_key(base_seed, dim, &k0, &k1);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  if ((rc = clear_status(c, st))) return rc;
-  const int64_t per = batch_runs(c, dim, 0);
+  const int64_t per = batch_runs(c, dim, 0) / 2;  // two record buffers in flight
   if (per < 1) return fail(c, JNE_ERR_BUDGET, "budget too small for one run");
   const double zscale = 1.0 / std::sqrt((double)steps);
+  cudaError_t e = cudaSuccess;
+  int last = -1;
+  // Batch b accumulates into record buffer b % 2 on `st` while the finalize of
+  // batch b - 1 runs on the context's second stream; events order the reuse.
   for (int64_t done = 0; done < n_runs; done += per) {
     const int n = (int)std::min<int64_t>(per, n_runs - done);
-    if ((rc = ensure(c, &c->d_mom, &c->mom_cap, (size_t)n * jne_record_slots(dim), "moment buffer"))) return rc;
-    if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr, st)))
+    const int b = (int)(c->batch_seq++ & 1);
+    if ((rc = ensure(c, &c->d_momb[b], &c->momb_cap[b], (size_t)n * jne_record_slots(dim), "moment buffer")))
       return rc;
-    if ((rc = finalize(c, model, dim, steps, n, zscale, out_device + (size_t)done * k, st))) return rc;
+    if (c->fin_pending[b] && (e = cudaStreamWaitEvent(st, c->ev_fin[b], 0)) != cudaSuccess)
+      return cuda_fail(c, e, "stream wait");
+    if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
+                         c->d_momb[b], st)))
+      return rc;
+    if ((e = cudaEventRecord(c->ev_acc[b], st)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(c->fin_stream, c->ev_acc[b], 0)) != cudaSuccess)
+      return cuda_fail(c, e, "stream order");
+    if ((rc = finalize(c, model, dim, steps, n, zscale, c->d_momb[b], out_device + (size_t)done * k,
+                       c->fin_stream)))
+      return rc;
+    if ((e = cudaEventRecord(c->ev_fin[b], c->fin_stream)) != cudaSuccess) return cuda_fail(c, e, "event record");
+    c->fin_pending[b] = true;
+    last = b;
   }
+  // later work on `st` sees the finished results
+  if (last >= 0 && (e = cudaStreamWaitEvent(st, c->ev_fin[last], 0)) != cudaSuccess)
+    return cuda_fail(c, e, "stream wait");
+  return JNE_OK;
+}
+
+int jne_sync(jne_context* c) {
+  if (!c) return JNE_ERR_ARG;
+  if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, JNE_ERR_CUDA, "cudaSetDevice failed");
+  cudaError_t e = cudaStreamSynchronize(c->fin_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   unsigned int stv = 0;
-  cudaError_t e = cudaMemcpyAsync(&stv, c->d_status, sizeof(stv), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return cuda_fail(c, e, "device batch");
+  if (e == cudaSuccess) e = cudaMemcpy(&stv, c->d_status, sizeof(stv), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned int));
+  if (e != cudaSuccess) return cuda_fail(c, e, "sync");
   if (stv & JNE_DEV_NOT_SPD) return fail(c, JNE_ERR_NUMERIC, "S11 not positive definite for some run (NaN written)");
   return JNE_OK;
 }

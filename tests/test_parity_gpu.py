@@ -118,6 +118,28 @@ def test_short_mixed_requests_run_fp64(engine):
     assert not np.array_equal(m, f) and normwise_err(m, f, 1.0) < tol_mixed(256)
 
 
+def test_device_path_matches_host_path(engine):
+    import torch
+
+    for prec in (0, 1):
+        ref = engine.eigs_seeded(4, 6, 2000, 3, 500, precision=prec)
+        out = torch.empty((500, 6), dtype=torch.float64, device="cuda")
+        engine.eigs_seeded_device(4, 6, 2000, 3, 500, out.data_ptr(), precision=prec)
+        engine.sync()
+        assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_device_path_reports_status_at_sync(engine, jne):
+    import torch
+
+    out = torch.empty((2, 1), dtype=torch.float64, device="cuda")
+    engine.eigs_seeded_device(0, 1, 1, 1, 2, out.data_ptr())  # S11 = 0: not positive definite
+    with pytest.raises(jne.JneError) as ei:
+        engine.sync()
+    assert ei.value.code == jne.JNE_ERR_NUMERIC
+    engine.sync()  # cleared
+
+
 def test_empty_batch(engine):
     assert engine.eigs_seeded(0, 3, 100, 1, 0).shape == (0, 3)
 
