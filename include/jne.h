@@ -105,6 +105,30 @@ int jne_eigs_seeded_models(jne_context* ctx, const int* models, int n_models, in
                            uint64_t base_seed, uint32_t seed_first, int64_t n_runs, int precision,
                            double* const* outs);
 
+/* No counterpart in the reference crate.  The seeded batch for callers that
+ * cannot allocate device memory -- a host framework that owns the GPU's
+ * allocator, a region being captured into a CUDA graph, a real-time loop that
+ * allows no allocation after start-up.  It needs no context: its scratch (the
+ * moment records and small tables) is one file-scope __device__ array of
+ * JNE_NOALLOC_SCRATCH_BYTES (4.7 MiB) that every GPU loading this library
+ * holds until the process exits, and it calls no cudaMalloc, cudaFree or
+ * allocating library routine.  Results go to out_device (n_runs x k doubles)
+ * on `stream` (a cudaStream_t; null = the legacy default stream); the call
+ * waits for them.  At most JNE_NOALLOC_MAX_RUNS runs per call (and, for mixed
+ * precision, at most JNE_NOALLOC_MAX_CHUNKS chunks: 1,048,576 steps), else
+ * JNE_ERR_BUDGET.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * whose GPU work overlaps (other threads or streams) race and must be
+ * serialised by the caller.  The message of a failed call comes from
+ * jne_noalloc_last_error (per thread). */
+#define JNE_NOALLOC_MAX_RUNS 2048
+#define JNE_NOALLOC_MAX_CHUNKS 4096
+#define JNE_NOALLOC_SCRATCH_BYTES 4956416
+int jne_eigs_seeded_noalloc(int device, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
+                            int n_runs, int precision, double* out_device, void* stream);
+const char* jne_noalloc_last_error(void);
+
 /* Per-kernel timing: when enabled, every kernel launch of ctx is bracketed by
  * CUDA events on its launching stream.  jne_profile_read returns the summed
  * device milliseconds and launch counts per kernel kind (index JNE_KERNEL_*),

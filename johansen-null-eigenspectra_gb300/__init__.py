@@ -33,6 +33,7 @@ EXPORTS = (
     "jne_export_increments", "jne_profile", "jne_profile_read", "jne_sync",
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
     "jne_simulation_filename", "jne_simulation_run", "jne_percentiles",
+    "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
 
