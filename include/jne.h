@@ -129,6 +129,30 @@ int jne_eigs_seeded_noalloc(int device, int model, int dim, int steps, uint64_t 
                             int n_runs, int precision, double* out_device, void* stream);
 const char* jne_noalloc_last_error(void);
 
+/* One request of a batch. */
+typedef struct jne_request {
+  int model, dim, steps, precision;
+  uint64_t base_seed;
+  uint32_t seed_first;
+  int64_t n_runs;
+} jne_request;
+
+/* A ragged batch: requests of any (model, dim, steps, seeds, size) in one
+ * persistent launch (the loop of the reference CLI over models and dims,
+ * src/main.rs:85-136, is one batch).  outs_device[i] receives request i's
+ * n_runs x k values.  Asynchronous, like jne_eigs_seeded_device. */
+int jne_run_batch(jne_context* ctx, const jne_request* reqs, int n_req, double* const* outs_device, void* stream);
+
+/* Plans: a ragged batch prepared once (device tables and records inside the
+ * context's budget) and captured into a CUDA graph; each jne_plan_launch
+ * replays it asynchronously on `stream`.  Requests must be mixed precision with
+ * steps >= JNE_MIXED_MIN_STEPS.  jne_plan_destroy waits for the last replay. */
+typedef struct jne_plan jne_plan;
+int jne_plan_create(jne_context* ctx, const jne_request* reqs, int n_req, double* const* outs_device,
+                    jne_plan** out);
+int jne_plan_launch(jne_plan* plan, void* stream);
+void jne_plan_destroy(jne_plan* plan);
+
 /* Per-kernel timing: when enabled, every kernel launch of ctx is bracketed by
  * CUDA events on its launching stream.  jne_profile_read returns the summed
  * device milliseconds and launch counts per kernel kind (index JNE_KERNEL_*),

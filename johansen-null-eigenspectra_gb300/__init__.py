@@ -34,8 +34,16 @@ EXPORTS = (
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
     "jne_simulation_filename", "jne_simulation_run", "jne_percentiles",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
+    "jne_run_batch", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
+
+
+class Request(ctypes.Structure):
+    """jne_request: one request of a batch (model, dim, steps, precision, seeds)."""
+
+    _fields_ = [("model", ctypes.c_int), ("dim", ctypes.c_int), ("steps", ctypes.c_int), ("precision", ctypes.c_int),
+                ("base_seed", ctypes.c_uint64), ("seed_first", ctypes.c_uint32), ("n_runs", ctypes.c_int64)]
 
 
 class JneError(RuntimeError):
@@ -134,6 +142,11 @@ def lib() -> ctypes.CDLL:
                                              c_int, ctypes.POINTER(dp)]
         L.jne_export_increments.argtypes = [vp, c_int, c_int, c_u64, c_u32, c_int, dp, ctypes.POINTER(c_u32)]
         L.jne_sync.argtypes = [vp]
+        L.jne_run_batch.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp), vp]
+        L.jne_plan_create.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+        L.jne_plan_launch.argtypes = [vp, vp]
+        L.jne_plan_destroy.argtypes = [vp]
+        L.jne_plan_destroy.restype = None
         L.jne_profile.argtypes = [vp, c_int]
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
@@ -230,6 +243,31 @@ class Engine:
         """Wait for all asynchronous work and raise on its device status (jne_sync)."""
         self._check(self._L.jne_sync(self._h))
 
+    @staticmethod
+    def _requests(reqs) -> "ctypes.Array":
+        arr = (Request * len(reqs))()
+        for i, r in enumerate(reqs):
+            d = dict(precision=PREC_MIXED, base_seed=DEFAULT_BASE_SEED, seed_first=1)
+            d.update(r)
+            arr[i] = Request(int(d["model"]), d["dim"], d["steps"], d["precision"], d["base_seed"], d["seed_first"],
+                             d["n_runs"])
+        return arr
+
+    def run_batch(self, reqs: Sequence[dict], out_ptrs: Sequence[int], stream: Optional[int] = None) -> None:
+        """jne_run_batch: a ragged batch (dicts with model, dim, steps, n_runs [, precision, seed_first,
+        base_seed]) into device buffers out_ptrs[i] (n_runs x k doubles each); asynchronous."""
+        arr = self._requests(reqs)
+        outs = (ctypes.c_void_p * len(reqs))(*[ctypes.c_void_p(p) for p in out_ptrs])
+        self._check(self._L.jne_run_batch(self._h, arr, len(reqs), outs, ctypes.c_void_p(stream or 0)))
+
+    def plan(self, reqs: Sequence[dict], out_ptrs: Sequence[int]) -> "Plan":
+        """jne_plan_create: the batch captured into a CUDA graph, replayed by Plan.launch()."""
+        arr = self._requests(reqs)
+        outs = (ctypes.c_void_p * len(reqs))(*[ctypes.c_void_p(p) for p in out_ptrs])
+        h = ctypes.c_void_p()
+        self._check(self._L.jne_plan_create(self._h, arr, len(reqs), outs, ctypes.byref(h)))
+        return Plan(self, h)
+
     def eigs_seeded_models(self, models: Sequence[int], dim: int, steps: int, seed_first: int, n_runs: int,
                            precision: int = PREC_FP64, base_seed: int = DEFAULT_BASE_SEED) -> Dict[int, np.ndarray]:
         outs = {int(m): np.empty((n_runs, eigen_count(m, dim))) for m in models}
@@ -246,6 +284,27 @@ class Engine:
         wp = w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)) if words else None
         self._check(self._L.jne_export_increments(self._h, dim, steps, base_seed, seed_first, n_runs, _dp(dB), wp))
         return dB, w
+
+
+class Plan:
+    """A captured ragged batch (jne_plan); launch() replays it asynchronously."""
+
+    def __init__(self, engine: Engine, handle: ctypes.c_void_p):
+        self._eng, self._h = engine, handle
+
+    def launch(self, stream: Optional[int] = None) -> None:
+        self._eng._check(self._eng._L.jne_plan_launch(self._h, ctypes.c_void_p(stream or 0)))
+
+    def destroy(self) -> None:
+        if self._h:
+            self._eng._L.jne_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 # --------------------------------------------------------------------------

@@ -142,44 +142,54 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
     for (int r = 0; r < 4; r++) acc[n][r] = __fadd_rn(acc[n][r], hh[n][r]);
 }
 
+// Per-warp shared memory of the accumulation (sized for the largest dim).
+constexpr int kRecMax = JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2 + 6 * JNE_MAX_DIM + JNE_MAX_DIM * JNE_MAX_DIM;
+struct alignas(16) WarpSmem {
+  float zs[16][kZS];      // increments of the current tile: z[feature][step]
+  float cm[16][kCS];      // the chunk's local Gram, staged for the merge
+  double wc[16], tz[16];  // walk at the chunk start, chunk increment totals
+  double rec[kRecMax];    // the run's record: FP64 part
+  float rech[kRecMax];    // ... and float-float centred part
+  float recl[kRecMax];
+  double mm[16], lm[16];  // per feature: chunk mean m, Lc * m
+  float sbf[16], tzfs[16], cub[16], cuub[16], cuz[16], cuuz[16];
+  unsigned short mww_pr[JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2];
+};
+
+// One run (seed a.seed_first + run) of a request: accumulate its moment record
+// into a.mom[slot * a.mom_ld + run].  Executed by a whole warp.
 template <int DIM, bool EXT>
-__global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4) k_accum_mixed(const jne_accum_args a) {
+__device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, WarpSmem& sm, const jne_round_keys& rk,
+                                          int lane) {
   constexpr int d = DIM;
   constexpr int NQ = (d + 3) / 4;
   constexpr int NMWW = d * (d + 1) / 2, NMW = 3 * d, NNZW = d * d;
   constexpr int NREC = NMWW + NMW + NNZW + 3 * d;  // == jne_record_slots(d)
-
-  __shared__ __align__(16) float zs_all[kMixWarps][16][kZS];
-  __shared__ float cm_all[kMixWarps][16][kCS];
-  __shared__ double wc_all[kMixWarps][16];
-  __shared__ double tz_all[kMixWarps][16];
-  __shared__ double rec_all[kMixWarps][NREC];   // the run's record: FP64 part
-  __shared__ float rech_all[kMixWarps][NREC];   // ... and float-float centred part
-  __shared__ float recl_all[kMixWarps][NREC];
-  __shared__ double fd_all[kMixWarps][2][16];   // per feature: chunk mean m, Lc * m
-  __shared__ float ff_all[kMixWarps][6][16];    // per feature: centred FP32 chunk moments
-  __shared__ unsigned short mww_pr[NMWW];
-
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int g = lane >> 2, q = lane & 3;
-  float (*zs)[kZS] = zs_all[wib];
-  float (*cm)[kCS] = cm_all[wib];
-  double* wc = wc_all[wib];
-  double* tz = tz_all[wib];
-  double* rec = rec_all[wib];
-  float* rech = rech_all[wib];
-  float* recl = recl_all[wib];
-  double* mm = fd_all[wib][0];
-  double* lm = fd_all[wib][1];
-  float* sbf = ff_all[wib][0];
-  float* tzfs = ff_all[wib][1];
-  float* cub = ff_all[wib][2];
-  float* cuub = ff_all[wib][3];
-  float* cuz = ff_all[wib][4];
-  float* cuuz = ff_all[wib][5];
-  for (int e = lane; e < 16 * kZS; e += 32) (&zs[0][0])[e] = 0.f;
-  if (lane < 16) tz[lane] = 0.0;
+  float (*zs)[kZS] = sm.zs;
+  float (*cm)[kCS] = sm.cm;
+  double* wc = sm.wc;
+  double* tz = sm.tz;
+  double* rec = sm.rec;
+  float* rech = sm.rech;
+  float* recl = sm.recl;
+  double* mm = sm.mm;
+  double* lm = sm.lm;
+  float* sbf = sm.sbf;
+  float* tzfs = sm.tzfs;
+  float* cub = sm.cub;
+  float* cuub = sm.cuub;
+  float* cuz = sm.cuz;
+  float* cuuz = sm.cuuz;
+  unsigned short* mww_pr = sm.mww_pr;
 
+  // rows d..15 of the staging area stay zero; (p, r) of the walk moments
+  for (int e = d * kZS + lane; e < 16 * kZS; e += 32) (&zs[0][0])[e] = 0.f;
+  for (int e = lane; e < NMWW; e += 32) {
+    int t = e, aa = 0;
+    while (t >= d - aa) { t -= d - aa; aa++; }
+    mww_pr[e] = (unsigned short)(aa | ((aa + t) << 8));
+  }
   // G-row coefficients: value = c[0]*b + c[1] + c[2]*u + c[3]*u^2
   float cA[4], cB[4];
   {
@@ -193,175 +203,214 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4) k_accum_mixed(const j
       cc[3] = rr == d + 2 ? 1.f : 0.f;
     }
   }
-  // (p, r) of the upper-triangular walk moments, shared by the block
-  for (int e = threadIdx.x; e < NMWW; e += blockDim.x) {
-    int t = e, aa = 0;
-    while (t >= d - aa) { t -= d - aa; aa++; }
-    mww_pr[e] = (unsigned short)(aa | ((aa + t) << 8));
-  }
-  __syncthreads();
-
   const int T = a.steps, L = a.chunk;
   const float invL = 1.0f / (float)L;
-  const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
   const float invTf = 1.0f / (float)T;
-  const int nwarps = gridDim.x * kMixWarps;
+  const uint32_t seed = a.seed_first + (uint32_t)run;
+  for (int e = lane; e < NREC; e += 32) {
+    rec[e] = 0.0;
+    rech[e] = 0.f;
+    recl[e] = 0.f;
+  }
+  if (lane < 16) {
+    wc[lane] = 0.0;
+    tz[lane] = 0.0;
+  }
+  __syncwarp();
 
-  for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps) {
-    const uint32_t seed = a.seed_first + (uint32_t)run;
+  for (int c0 = 0; c0 < T; c0 += L) {
+    const int Lc = min(L, T - c0);
+    float acc[4][4], accx[4][4];  // chunk sums: hi*hi (emptied per tile) and cross terms
+#pragma unroll
+    for (int n = 0; n < 4; n++)
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        acc[n][r] = 0.f;
+        accx[n][r] = 0.f;
+      }
+    float chiA = 0.f, cloA = 0.f, chiB = 0.f, cloB = 0.f;
+
+    for (int t0 = c0; t0 < c0 + Lc; t0 += 32) {
+      // producer: lane = tile step, all d increments of column t0 + lane
+      const int i = t0 + lane;
+      const bool valid = i < T;
+      if (EXT) {
+        const double* src = a.ext + ((size_t)run * T + (valid ? i : 0)) * d;
+#pragma unroll
+        for (int f = 0; f < d; f++) zs[f][lane] = valid ? (float)(src[f] * a.ext_inv_scale) : 0.f;
+      } else {
+#pragma unroll
+        for (int j = 0; j < NQ; j++) {
+          float z[4];
+          jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, rk, z);
+#pragma unroll
+          for (int e = 0; e < 4; e++)
+            if (4 * j + e < d) zs[4 * j + e][lane] = valid ? z[e] : 0.f;
+        }
+      }
+      __syncwarp();
+      const int nvalid = min(32, T - t0);
+      const int tloc = t0 - c0 + 8 * q;
+      if (nvalid == 32)
+        tile_body<DIM, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
+      else
+        tile_body<DIM, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
+      __syncwarp();
+    }
+
+    // ---- chunk end: stage the local Gram and the chunk totals ----
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      cm[g][8 * n + 2 * q] = acc[n][0] + accx[n][0];
+      cm[g][8 * n + 2 * q + 1] = acc[n][1] + accx[n][1];
+      cm[g + 8][8 * n + 2 * q] = acc[n][2] + accx[n][2];
+      cm[g + 8][8 * n + 2 * q + 1] = acc[n][3] + accx[n][3];
+    }
+    if (q == 0) {
+      if (g < d) tz[g] = (double)chiA + (double)cloA;
+      if (g + 8 < d) tz[g + 8] = (double)chiB + (double)cloB;
+    }
+    __syncwarp();
+    // ---- merge into the run's record: W = m + beta (m = chunk mean of W, sum beta = 0),
+    //      y = ybar + h (u - ubar).  Every moment splits into a "mean" part, a product of
+    //      chunk means (FP64, one FMA per slot), and a centred local part (FP32, small,
+    //      summed across chunks in float-float). ----
+    const jne_chunk_time ct = a.chunk_tab[c0 / L];
+    const float Lcf = (float)Lc, invLcf = 1.0f / Lcf;
+    const float P1f = 0.5f * Lcf * (Lcf - 1.0f) * invL;
+    const float P2f = (Lcf - 1.0f) * Lcf * (2.0f * Lcf - 1.0f) * invL * invL * (1.0f / 6.0f);
+    const float ub = P1f * invLcf;                 // mean of u over the chunk
+    const float sig2 = P2f - P1f * ub;             // sum of (u - ubar)^2
+    const float qbar = sig2 * invLcf;              // mean of (u - ubar)^2
+    const float hf = (float)L * invTf, ybf = (float)ct.ybar;
+    if (lane < d) {
+      const int f = lane;
+      const float Sb = cm[d][f], Sub = cm[d + 1][f], Suub = cm[d + 2][f];
+      const float Suz = cm[d + 1][16 + f], Suuz = cm[d + 2][16 + f];
+      const double m = wc[f] + (double)Sb * ct.inv_lc;
+      mm[f] = m;
+      lm[f] = ct.lc * m;
+      const float tzf = (float)tz[f];
+      sbf[f] = Sb;
+      tzfs[f] = tzf;
+      cub[f] = Sub - ub * Sb;                                              // sum (u-ubar) beta
+      cuub[f] = Suub - 2.0f * ub * Sub + ub * ub * Sb - Sb * invLcf * sig2;  // sum (u-ubar)^2 beta
+      cuz[f] = Suz - ub * tzf;                                             // sum (u-ubar) z
+      cuuz[f] = Suuz - 2.0f * ub * Suz + ub * ub * tzf - qbar * tzf;       // sum ((u-ubar)^2 - qbar) z
+    }
+    __syncwarp();
+    // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy
     for (int e = lane; e < NREC; e += 32) {
-      rec[e] = 0.0;
-      rech[e] = 0.f;
-      recl[e] = 0.f;
-    }
-    if (lane < 16) wc[lane] = 0.0;
-    __syncwarp();
-
-    for (int c0 = 0; c0 < T; c0 += L) {
-      const int Lc = min(L, T - c0);
-      float acc[4][4], accx[4][4];  // chunk sums: hi*hi (emptied per tile) and cross terms
-#pragma unroll
-      for (int n = 0; n < 4; n++)
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-          acc[n][r] = 0.f;
-          accx[n][r] = 0.f;
-        }
-      float chiA = 0.f, cloA = 0.f, chiB = 0.f, cloB = 0.f;
-
-      for (int t0 = c0; t0 < c0 + Lc; t0 += 32) {
-        // producer: lane = tile step, all d increments of column t0 + lane
-        const int i = t0 + lane;
-        const bool valid = i < T;
-        if (EXT) {
-          const double* src = a.ext + ((size_t)run * T + (valid ? i : 0)) * d;
-#pragma unroll
-          for (int f = 0; f < d; f++) zs[f][lane] = valid ? (float)(src[f] * a.ext_inv_scale) : 0.f;
-        } else {
-#pragma unroll
-          for (int j = 0; j < NQ; j++) {
-            float z[4];
-            jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, rk, z);
-#pragma unroll
-            for (int e = 0; e < 4; e++)
-              if (4 * j + e < d) zs[4 * j + e][lane] = valid ? z[e] : 0.f;
-          }
-        }
-        __syncwarp();
-        const int nvalid = min(32, T - t0);
-        const int tloc = t0 - c0 + 8 * q;
-        if (nvalid == 32)
-          tile_body<DIM, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
-        else
-          tile_body<DIM, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
-        __syncwarp();
-      }
-
-      // ---- chunk end: stage the local Gram and the chunk totals ----
-#pragma unroll
-      for (int n = 0; n < 4; n++) {
-        cm[g][8 * n + 2 * q] = acc[n][0] + accx[n][0];
-        cm[g][8 * n + 2 * q + 1] = acc[n][1] + accx[n][1];
-        cm[g + 8][8 * n + 2 * q] = acc[n][2] + accx[n][2];
-        cm[g + 8][8 * n + 2 * q + 1] = acc[n][3] + accx[n][3];
-      }
-      if (q == 0) {
-        if (g < d) tz[g] = (double)chiA + (double)cloA;
-        if (g + 8 < d) tz[g + 8] = (double)chiB + (double)cloB;
-      }
-      __syncwarp();
-      // ---- merge into the run's record: W = m + beta (m = chunk mean of W, sum beta = 0),
-      //      y = ybar + h (u - ubar).  Every moment splits into a "mean" part, a product of
-      //      chunk means (FP64, one FMA per slot), and a centred local part (FP32, small,
-      //      summed across chunks in float-float). ----
-      const jne_chunk_time ct = a.chunk_tab[c0 / L];
-      const float Lcf = (float)Lc, invLcf = 1.0f / Lcf;
-      const float P1f = 0.5f * Lcf * (Lcf - 1.0f) * invL;
-      const float P2f = (Lcf - 1.0f) * Lcf * (2.0f * Lcf - 1.0f) * invL * invL * (1.0f / 6.0f);
-      const float ub = P1f * invLcf;                 // mean of u over the chunk
-      const float sig2 = P2f - P1f * ub;             // sum of (u - ubar)^2
-      const float qbar = sig2 * invLcf;              // mean of (u - ubar)^2
-      const float hf = (float)L * invTf, ybf = (float)ct.ybar;
-      if (lane < d) {
-        const int f = lane;
-        const float Sb = cm[d][f], Sub = cm[d + 1][f], Suub = cm[d + 2][f];
-        const float Suz = cm[d + 1][16 + f], Suuz = cm[d + 2][16 + f];
-        const double m = wc[f] + (double)Sb * ct.inv_lc;
-        mm[f] = m;
-        lm[f] = ct.lc * m;
-        const float tzf = (float)tz[f];
-        sbf[f] = Sb;
-        tzfs[f] = tzf;
-        cub[f] = Sub - ub * Sb;                                              // sum (u-ubar) beta
-        cuub[f] = Suub - 2.0f * ub * Sub + ub * ub * Sb - Sb * invLcf * sig2;  // sum (u-ubar)^2 beta
-        cuz[f] = Suz - ub * tzf;                                             // sum (u-ubar) z
-        cuuz[f] = Suuz - 2.0f * ub * Suz + ub * ub * tzf - qbar * tzf;       // sum ((u-ubar)^2 - qbar) z
-      }
-      __syncwarp();
-      // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy
-      for (int e = lane; e < NREC; e += 32) {
-        double v64;
-        float v32;
-        if (e < NMWW) {
-          const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
-          v64 = lm[p] * mm[r];
-          v32 = cm[p][r] - sbf[p] * sbf[r] * invLcf;
-        } else if (e < NMWW + NMW) {
-          const int t = e - NMWW, pp = t / d, r = t - pp * d;
-          if (pp == 0) {
-            v64 = lm[r];
-            v32 = 0.f;
-          } else if (pp == 1) {
-            v64 = ct.ybar * lm[r];
-            v32 = hf * cub[r];
-          } else {
-            v64 = ct.y2bar * lm[r];
-            v32 = 2.0f * ybf * hf * cub[r] + hf * hf * cuub[r];
-          }
-        } else if (e < NMWW + NMW + NNZW) {
-          const int t = e - NMWW - NMW, za = t / d, wb = t - za * d;
-          v64 = tz[za] * mm[wb];
-          v32 = cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf;
-        } else if (e < NMWW + NMW + NNZW + d) {
-          v64 = 0.0;  // Nz1: the walk's end point, written from wc
+      double v64;
+      float v32;
+      if (e < NMWW) {
+        const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
+        v64 = lm[p] * mm[r];
+        v32 = cm[p][r] - sbf[p] * sbf[r] * invLcf;
+      } else if (e < NMWW + NMW) {
+        const int t = e - NMWW, pp = t / d, r = t - pp * d;
+        if (pp == 0) {
+          v64 = lm[r];
           v32 = 0.f;
+        } else if (pp == 1) {
+          v64 = ct.ybar * lm[r];
+          v32 = hf * cub[r];
         } else {
-          const int t = e - NMWW - NMW - NNZW - d, pp = 1 + t / d, za = t - (pp - 1) * d;
-          if (pp == 1) {
-            v64 = ct.ybar * tz[za];
-            v32 = hf * cuz[za];
-          } else {
-            v64 = ct.y2bar * tz[za];
-            v32 = 2.0f * ybf * hf * cuz[za] + hf * hf * cuuz[za];
-          }
+          v64 = ct.y2bar * lm[r];
+          v32 = 2.0f * ybf * hf * cub[r] + hf * hf * cuub[r];
         }
-        rec[e] += v64;
-        ff_add(rech[e], recl[e], v32);
+      } else if (e < NMWW + NMW + NNZW) {
+        const int t = e - NMWW - NMW, za = t / d, wb = t - za * d;
+        v64 = tz[za] * mm[wb];
+        v32 = cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf;
+      } else if (e < NMWW + NMW + NNZW + d) {
+        v64 = 0.0;  // Nz1: the walk's end point, written from wc
+        v32 = 0.f;
+      } else {
+        const int t = e - NMWW - NMW - NNZW - d, pp = 1 + t / d, za = t - (pp - 1) * d;
+        if (pp == 1) {
+          v64 = ct.ybar * tz[za];
+          v32 = hf * cuz[za];
+        } else {
+          v64 = ct.y2bar * tz[za];
+          v32 = 2.0f * ybf * hf * cuz[za] + hf * hf * cuuz[za];
+        }
       }
-      __syncwarp();
-      if (lane < d) wc[lane] += tz[lane];
-      __syncwarp();
+      rec[e] += v64;
+      ff_add(rech[e], recl[e], v32);
     }
+    __syncwarp();
+    if (lane < d) wc[lane] += tz[lane];
+    __syncwarp();
+  }
 
-    // ---- write the record (slot order of jne_common.cuh) ----
-    if (lane < d) rec[jne_slot_Nz1(lane, d)] = wc[lane];
-    __syncwarp();
-    const size_t ld = (size_t)a.mom_ld;
-    for (int e = lane; e < NREC; e += 32) a.mom[(size_t)e * ld + run] = rec[e] + ((double)rech[e] + (double)recl[e]);
-    __syncwarp();
+  // ---- write the record (slot order of jne_common.cuh) ----
+  if (lane < d) rec[jne_slot_Nz1(lane, d)] = wc[lane];
+  __syncwarp();
+  const size_t ld = (size_t)a.mom_ld;
+  for (int e = lane; e < NREC; e += 32) a.mom[(size_t)e * ld + run] = rec[e] + ((double)rech[e] + (double)recl[e]);
+  __syncwarp();
+}
+
+// One request: every warp strides over its runs.
+template <int DIM, bool EXT>
+__global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4) k_accum_mixed(const jne_accum_args a) {
+  __shared__ WarpSmem sm_all[kMixWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
+  const int nwarps = gridDim.x * kMixWarps;
+  for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps)
+    accum_run<DIM, EXT>(a, run, sm_all[wib], rk, lane);
+}
+
+// A ragged batch of requests (any dims, step counts and sizes) in one
+// persistent launch: each warp takes the next run of the flattened batch from
+// a global counter, so long and short requests share the GPU without tails.
+__global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
+    k_accum_mixed_ragged(const jne_ragged_req* __restrict__ reqs, int n_req, long long total,
+                         unsigned long long* __restrict__ counter) {
+  __shared__ WarpSmem sm_all[kMixWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  for (;;) {
+    unsigned long long item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1ull);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= (unsigned long long)total) break;
+    int lo = 0, hi = n_req - 1;  // request r with reqs[r].first <= item < reqs[r + 1].first
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if ((unsigned long long)reqs[mid].first <= item) lo = mid; else hi = mid - 1;
+    }
+    const jne_accum_args& a = reqs[lo].acc;
+    const int run = (int)(item - (unsigned long long)reqs[lo].first);
+    const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
+    switch (a.dim) {
+      case 1: accum_run<1, false>(a, run, sm_all[wib], rk, lane); break;
+      case 2: accum_run<2, false>(a, run, sm_all[wib], rk, lane); break;
+      case 3: accum_run<3, false>(a, run, sm_all[wib], rk, lane); break;
+      case 4: accum_run<4, false>(a, run, sm_all[wib], rk, lane); break;
+      case 5: accum_run<5, false>(a, run, sm_all[wib], rk, lane); break;
+      case 6: accum_run<6, false>(a, run, sm_all[wib], rk, lane); break;
+      case 7: accum_run<7, false>(a, run, sm_all[wib], rk, lane); break;
+      case 8: accum_run<8, false>(a, run, sm_all[wib], rk, lane); break;
+      case 9: accum_run<9, false>(a, run, sm_all[wib], rk, lane); break;
+      case 10: accum_run<10, false>(a, run, sm_all[wib], rk, lane); break;
+      case 11: accum_run<11, false>(a, run, sm_all[wib], rk, lane); break;
+      default: accum_run<12, false>(a, run, sm_all[wib], rk, lane); break;
+    }
   }
 }
 
 // Persistent grid: exactly the resident blocks (so every warp strides over the
 // same number of runs, +-1), or fewer when the batch is small.
 template <typename K>
-int resident_grid(K kernel, int threads, size_t shm, int sms, int n_runs, int warps_per_block) {
+int resident_grid(K kernel, int threads, size_t shm, int sms, long long n_runs, int warps_per_block) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, shm) != cudaSuccess || per_sm < 1)
     per_sm = 1;
-  const int needed = (n_runs + warps_per_block - 1) / warps_per_block;
-  const int full = per_sm * sms;
-  return needed < full ? needed : full;
+  const long long needed = (n_runs + warps_per_block - 1) / warps_per_block;
+  const long long full = (long long)per_sm * sms;
+  return (int)(needed < full ? needed : full);
 }
 
 template <int DIM>
@@ -378,6 +427,15 @@ cudaError_t launch_dim(const jne_accum_args& a, int sms, cudaStream_t st) {
 }
 
 }  // namespace
+
+cudaError_t jne_launch_accum_mixed_ragged(const jne_ragged_req* reqs, int n_req, long long total,
+                                         unsigned long long* counter, int sms, cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  const int threads = kMixWarps * JNE_WARP;
+  k_accum_mixed_ragged<<<resident_grid(k_accum_mixed_ragged, threads, 0, sms, total, kMixWarps), threads, 0, st>>>(
+      reqs, n_req, total, counter);
+  return cudaGetLastError();
+}
 
 cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, int sms, cudaStream_t st) {
   if (a.n_runs <= 0) return cudaSuccess;

@@ -129,9 +129,7 @@ __device__ bool tridiagonal_ql(double* dg, double* eo, int n) {
   return ok;
 }
 
-__global__ void __launch_bounds__(kFinThreads) k_finalize(const jne_finalize_args f) {
-  const int run = blockIdx.x * kFinThreads + threadIdx.x;
-  if (run >= f.n_runs) return;
+__device__ void finalize_run(const jne_finalize_args& f, int run) {
   const int d = f.dim, model = f.model;
   const int k = (model == 1 || model == 3) ? d + 1 : d;
   const Ctx c{f.mom, f.mom_ld, run, d, f.zscale, f.ts.Y};
@@ -222,7 +220,35 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(const jne_finalize_arg
   for (int j = 0; j < k; j++) out[j] = dg[j];
 }
 
+__global__ void __launch_bounds__(kFinThreads) k_finalize(const jne_finalize_args f) {
+  const int run = blockIdx.x * kFinThreads + threadIdx.x;
+  if (run < f.n_runs) finalize_run(f, run);
+}
+
+// Every run of a ragged batch, one thread each.
+__global__ void __launch_bounds__(kFinThreads)
+    k_finalize_ragged(const jne_ragged_req* __restrict__ reqs, int n_req, long long total) {
+  const long long item = (long long)blockIdx.x * kFinThreads + threadIdx.x;
+  if (item >= total) return;
+  int lo = 0, hi = n_req - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (reqs[mid].first <= item) lo = mid; else hi = mid - 1;
+  }
+  finalize_run(reqs[lo].fin, (int)(item - reqs[lo].first));
+}
+
 }  // namespace
+
+cudaError_t jne_launch_finalize_ragged(const jne_ragged_req* reqs, int n_req, long long total, int sms,
+                                       cudaStream_t st) {
+  (void)sms;
+  if (total <= 0) return cudaSuccess;
+  const long long grid = (total + kFinThreads - 1) / kFinThreads;
+  if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+  k_finalize_ragged<<<(unsigned)grid, kFinThreads, 0, st>>>(reqs, n_req, total);
+  return cudaGetLastError();
+}
 
 cudaError_t jne_launch_finalize(const jne_finalize_args& f, int sms, cudaStream_t st) {
   (void)sms;

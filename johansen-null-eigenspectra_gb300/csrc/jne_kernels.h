@@ -19,6 +19,19 @@ struct jne_finalize_args {
   unsigned int* status;
 };
 
+// One request of a ragged batch, as the device sees it: the accumulation and
+// finalize argument blocks and the request's first index in the flattened run
+// space of the batch.
+struct jne_ragged_req {
+  jne_accum_args acc;
+  jne_finalize_args fin;
+  long long first;
+};
+
+cudaError_t jne_launch_accum_mixed_ragged(const jne_ragged_req* reqs, int n_req, long long total,
+                                         unsigned long long* counter, int sms, cudaStream_t st);
+cudaError_t jne_launch_finalize_ragged(const jne_ragged_req* reqs, int n_req, long long total, int sms,
+                                       cudaStream_t st);
 cudaError_t jne_launch_accum_f64(const jne_accum_args& a, const int4* ent, int nent, int sms, cudaStream_t st);
 int jne_build_f64_entries(int model, int d, int4* out, int cap);
 cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, int sms, cudaStream_t st);

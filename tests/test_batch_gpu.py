@@ -1,0 +1,91 @@
+"""Ragged batches (one persistent launch over mixed requests) and plans (a batch
+captured into a CUDA graph and replayed): each request's result must equal the
+single-request path, and be the same alone and in any mix."""
+import numpy as np
+import pytest
+
+from conftest import normwise_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _outs(jne, reqs):
+    import torch
+
+    return [torch.full((r["n_runs"], jne.eigen_count(r["model"], r["dim"])), float("nan"), dtype=torch.float64,
+                       device="cuda") for r in reqs]
+
+
+MIX = [
+    dict(model=0, dim=12, steps=1000, n_runs=300),
+    dict(model=4, dim=3, steps=2500, n_runs=57, seed_first=1000),
+    dict(model=1, dim=1, steps=300, n_runs=1000),
+    dict(model=3, dim=7, steps=777, n_runs=130, base_seed=99),
+    dict(model=2, dim=12, steps=4096, n_runs=64, seed_first=5),
+    dict(model=2, dim=5, steps=100, n_runs=40),                    # short path: FP64 kernel
+    dict(model=4, dim=9, steps=600, n_runs=33, precision=0),       # FP64 request
+    dict(model=0, dim=2, steps=500, n_runs=0),                     # empty
+]
+
+
+def _single(engine, jne, r):
+    return engine.eigs_seeded(r["model"], r["dim"], r["steps"], r.get("seed_first", 1), r["n_runs"],
+                              precision=r.get("precision", jne.PREC_MIXED),
+                              base_seed=r.get("base_seed", jne.DEFAULT_BASE_SEED))
+
+
+def test_ragged_batch_matches_single_requests(engine, jne):
+    outs = _outs(jne, MIX)
+    engine.run_batch(MIX, [o.data_ptr() for o in outs])
+    engine.sync()
+    for r, o in zip(MIX, outs):
+        ref = _single(engine, jne, r)
+        got = o.cpu().numpy()
+        assert got.shape == ref.shape
+        if r["n_runs"]:
+            assert normwise_err(got, ref, 1.0) < 1e-12, r
+
+
+def test_result_same_alone_and_in_the_mix(engine, jne):
+    alone = _outs(jne, MIX[:1])
+    engine.run_batch(MIX[:1], [alone[0].data_ptr()])
+    mixed = _outs(jne, MIX)
+    engine.run_batch(MIX[::-1], [o.data_ptr() for o in mixed[::-1]])  # other order, other neighbours
+    engine.sync()
+    assert np.array_equal(alone[0].cpu().numpy(), mixed[0].cpu().numpy())
+
+
+def test_batches_split_across_launches_under_a_small_budget(jne):
+    reqs = [dict(model=m, dim=12, steps=512, n_runs=3000) for m in range(5)]
+    with jne.Engine(0, mem_budget_bytes=64 << 20) as small, jne.Engine(0) as big:
+        a, b = _outs(jne, reqs), _outs(jne, reqs)
+        small.run_batch(reqs, [o.data_ptr() for o in a])  # ~7 MB of records per request: several launches
+        big.run_batch(reqs, [o.data_ptr() for o in b])
+        small.sync()
+        big.sync()
+        for x, y in zip(a, b):
+            assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+
+
+def test_plan_replays_the_batch(engine, jne):
+    reqs = [r for r in MIX[:5]]
+    ref = _outs(jne, reqs)
+    engine.run_batch(reqs, [o.data_ptr() for o in ref])
+    engine.sync()
+    outs = _outs(jne, reqs)
+    plan = engine.plan(reqs, [o.data_ptr() for o in outs])
+    for _ in range(3):
+        plan.launch()
+        engine.sync()
+        for x, y in zip(outs, ref):
+            assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+        for o in outs:
+            o.fill_(float("nan"))
+    plan.destroy()
+
+
+def test_plan_rejects_fp64_requests(engine, jne):
+    reqs = [dict(model=0, dim=2, steps=1000, n_runs=10, precision=0)]
+    with pytest.raises(jne.JneError) as ei:
+        engine.plan(reqs, [o.data_ptr() for o in _outs(jne, reqs)])
+    assert ei.value.code == jne.JNE_ERR_ARG
