@@ -271,6 +271,9 @@ def run_gpu(args, rank: int, world: int) -> None:
              "frac": normals_rate / args.rng_peak,
              "note": "Philox4x32-10 + Box-Muller rate measured by a standalone throughput kernel on GB300"}
 
+    ragged = bench_ragged60(jne, torch, local, args.ragged_steps) if args.ragged_steps > 0 and rank == 0 else None
+    serving = bench_serving(jne, local, args.serve_seconds) if args.serve_seconds > 0 and rank == 0 else None
+
     cpu = None
     if rank == 0 and args.cpu_runs != 0:
         oracle = entry.load_oracle()
@@ -299,11 +302,91 @@ def run_gpu(args, rank: int, world: int) -> None:
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
             "gpu_launches": acc_n + fin_n,
             "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
+            "ragged60": ragged, "serving": serving,
             "cpu_baseline": cpu, "clocks": clk.summary(),
         }))
     eng.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def ragged60_requests(seed: int = 0xC4):
+    """All 60 (model, dim) pairs; T from {1000, 5000, 10000} and runs log-uniform in [1e4, 1e6], per pair."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for model in MODELS:
+        for dim in range(1, 13):
+            reqs.append(dict(model=model, dim=dim, steps=int(rng.choice([1000, 5000, 10000])),
+                             n_runs=int(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))))
+    return reqs
+
+
+def bench_ragged60(jne, torch, local: int, steps: int) -> dict:
+    """One persistent launch over the ragged 60-pair batch, captured as a CUDA graph and replayed."""
+    reqs = ragged60_requests()
+    total = sum(r["n_runs"] for r in reqs)
+    outs = [torch.empty((r["n_runs"], jne.eigen_count(r["model"], r["dim"])), dtype=torch.float64, device="cuda")
+            for r in reqs]
+    with jne.Engine(local) as eng:
+        plan = eng.plan(reqs, [o.data_ptr() for o in outs])
+        stream = torch.cuda.Stream()
+        plan.launch(stream.cuda_stream)  # warm-up replay
+        eng.sync()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            plan.launch(stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        eng.sync()
+        ms = a.elapsed_time(b) / steps
+        plan.destroy()
+    finite = all(bool(torch.isfinite(o).all()) for o in outs)
+    return {"runs_per_s": total / (ms * 1e-3), "ms_per_replay": ms, "requests": len(reqs), "total_runs": total,
+            "replays": steps, "all_finite": finite, "graph": True,
+            "workload": "60 (model, dim) pairs, T in {1000,5000,10000} and runs log-uniform [1e4,1e6] per pair "
+                        "(seed 0xC4), mixed precision, one persistent ragged launch + ragged finalize per replay"}
+
+
+def bench_serving(jne, local: int, seconds: float, rate: float = 200.0, seed: int = 0xC5) -> dict:
+    """Poisson arrivals (mean `rate` req/s) for `seconds`; model U{0..4}, dim U{1..12}, T log-U[500, 2e4],
+    runs log-U[1e3, 1e6], per-request seed; 40 GB budget; latency = finish - submit."""
+    rng = np.random.default_rng(seed)
+    arrivals, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        arrivals.append((t, dict(model=int(rng.integers(0, 5)), dim=int(rng.integers(1, 13)),
+                                 steps=int(np.exp(rng.uniform(np.log(500), np.log(2e4)))),
+                                 n_runs=int(np.exp(rng.uniform(np.log(1e3), np.log(1e6)))),
+                                 base_seed=int(rng.integers(1, 2**62)))))
+    total_runs = sum(r["n_runs"] for _, r in arrivals)
+    with jne.Engine(local, mem_budget_bytes=40 << 30) as eng:
+        with jne.Server(eng) as srv:
+            t0 = time.perf_counter()
+            ids = []
+            for at, r in arrivals:
+                delay = at - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append(srv.submit(**r))
+            done = {}
+            while len(done) < len(ids):
+                for c in srv.wait(timeout_ms=120_000):
+                    done[c.id] = c
+            for i in ids:
+                srv.fetch(i)
+    lat = np.array([done[i].finish_s - done[i].submit_s for i in ids])
+    span = max(c.finish_s for c in done.values()) - min(c.submit_s for c in done.values())
+    ok = sum(1 for c in done.values() if c.status == jne.JNE_OK)
+    return {"requests": len(ids), "ok": ok, "offered_req_per_s": rate, "arrival_seconds": seconds,
+            "total_runs": total_runs, "runs_per_s": total_runs / span, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "makespan_s": span,
+            "workload": "Poisson 200 req/s; model U{0..4}, dim U{1..12}, T log-U[500,2e4], runs log-U[1e3,1e6], "
+                        "per-request seed; continuous batching, 40 GB budget, mixed precision"}
 
 
 def main() -> None:
@@ -318,6 +401,8 @@ def main() -> None:
     ap.add_argument("--cpu-runs", type=int, default=None, help="CPU sample runs per model (0 = skip)")
     ap.add_argument("--chunk", type=int, default=0, help="steps per FP32 chunk (0: adaptive, 256 at T=10k)")
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per accumulation launch")
+    ap.add_argument("--ragged-steps", type=int, default=2, help="timed replays of the ragged 60-pair plan (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="Poisson arrival window of the serving run (0: skip)")
     ap.add_argument("--rng-peak", type=float, default=1.016e12, help="measured Philox+Box-Muller normals/s")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))

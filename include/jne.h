@@ -153,6 +153,33 @@ int jne_plan_create(jne_context* ctx, const jne_request* reqs, int n_req, double
 int jne_plan_launch(jne_plan* plan, void* stream);
 void jne_plan_destroy(jne_plan* plan);
 
+/* ---- continuous-batching request loop (serving) ----
+ * A worker thread owns the context while the server is open (do not call other
+ * jne_* functions on that context meanwhile).  Requests are admitted FIFO while
+ * their device output buffers fit half the context's budget; every iteration is
+ * one ragged launch over a slice of each active request (about iter_work
+ * runs x steps in total, 0 = 2e9), so new requests join running ones at the
+ * next iteration.  Finished results wait in host memory for jne_server_fetch;
+ * with a data directory they are also streamed, by a writer thread, to
+ * <data_dir>/request<id>_model<m>_dim<d>_steps<T>.dat (EIGENVALS_V6). */
+typedef struct jne_server jne_server;
+typedef struct jne_completion {
+  uint64_t id;
+  int status;                           /* JNE_OK or the request's error */
+  double submit_s, start_s, finish_s;  /* seconds since jne_server_open */
+  int64_t n_runs;
+} jne_completion;
+int jne_server_open(jne_context* ctx, const char* data_dir, long long iter_work, jne_server** out);
+int jne_server_submit(jne_server* server, const jne_request* req, uint64_t* id);
+/* Up to max completions into out (*n of them), waiting up to timeout_ms (-1: no limit) for the first. */
+int jne_server_wait(jne_server* server, jne_completion* out, int max, int timeout_ms, int* n);
+/* Copies a finished request's n_runs x k eigenvalues (host) and forgets the
+ * request; returns its status, JNE_ERR_ARG for an unknown or unfinished id or a
+ * short buffer, JNE_ERR_TIMEOUT while its file is still being written. */
+int jne_server_fetch(jne_server* server, uint64_t id, double* out, int64_t cap);
+/* Finishes every submitted request, then stops the worker and writer threads. */
+int jne_server_close(jne_server* server);
+
 /* Per-kernel timing: when enabled, every kernel launch of ctx is bracketed by
  * CUDA events on its launching stream.  jne_profile_read returns the summed
  * device milliseconds and launch counts per kernel kind (index JNE_KERNEL_*),

@@ -35,6 +35,7 @@ EXPORTS = (
     "jne_simulation_filename", "jne_simulation_run", "jne_percentiles",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
     "jne_run_batch", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
+    "jne_server_open", "jne_server_submit", "jne_server_wait", "jne_server_fetch", "jne_server_close",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
 
@@ -44,6 +45,13 @@ class Request(ctypes.Structure):
 
     _fields_ = [("model", ctypes.c_int), ("dim", ctypes.c_int), ("steps", ctypes.c_int), ("precision", ctypes.c_int),
                 ("base_seed", ctypes.c_uint64), ("seed_first", ctypes.c_uint32), ("n_runs", ctypes.c_int64)]
+
+
+class Completion(ctypes.Structure):
+    """jne_completion: a finished request of the server, with its times (seconds since the server opened)."""
+
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("finish_s", ctypes.c_double), ("n_runs", ctypes.c_int64)]
 
 
 class JneError(RuntimeError):
@@ -147,6 +155,11 @@ def lib() -> ctypes.CDLL:
         L.jne_plan_launch.argtypes = [vp, vp]
         L.jne_plan_destroy.argtypes = [vp]
         L.jne_plan_destroy.restype = None
+        L.jne_server_open.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong, ctypes.POINTER(vp)]
+        L.jne_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(c_u64)]
+        L.jne_server_wait.argtypes = [vp, ctypes.POINTER(Completion), c_int, c_int, ctypes.POINTER(c_int)]
+        L.jne_server_fetch.argtypes = [vp, c_u64, dp, c_i64]
+        L.jne_server_close.argtypes = [vp]
         L.jne_profile.argtypes = [vp, c_int]
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
@@ -305,6 +318,56 @@ class Plan:
             self.destroy()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching request loop on an engine (jne_server_*).  While it is
+    open, its worker thread owns the engine's context."""
+
+    def __init__(self, engine: Engine, data_dir: Optional[str] = None, iter_work: int = 0):
+        self._eng, self._L = engine, engine._L
+        h = ctypes.c_void_p()
+        engine._check(self._L.jne_server_open(engine._h, os.fsencode(data_dir) if data_dir else None, iter_work,
+                                              ctypes.byref(h)))
+        self._h = h
+        self._k: Dict[int, int] = {}
+
+    def submit(self, model: int, dim: int, steps: int, n_runs: int, seed_first: int = 1,
+               base_seed: int = DEFAULT_BASE_SEED, precision: int = PREC_MIXED) -> int:
+        r = Request(int(model), dim, steps, precision, base_seed, seed_first, n_runs)
+        rid = ctypes.c_uint64()
+        rc = self._L.jne_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid))
+        if rc != JNE_OK:
+            raise JneError(rc, "request rejected")
+        self._k[rid.value] = (n_runs, eigen_count(model, dim))
+        return rid.value
+
+    def wait(self, max_n: int = 256, timeout_ms: int = -1) -> List[Completion]:
+        buf = (Completion * max_n)()
+        n = ctypes.c_int()
+        self._eng._check(self._L.jne_server_wait(self._h, buf, max_n, timeout_ms, ctypes.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def fetch(self, rid: int) -> np.ndarray:
+        n, k = self._k.pop(rid)
+        out = np.empty((n, k))
+        rc = self._L.jne_server_fetch(self._h, rid, _dp(out), out.size)
+        if rc != JNE_OK:
+            if rc in (JNE_ERR_ARG, JNE_ERR_TIMEOUT):  # not finished / still being written: fetch again
+                self._k[rid] = (n, k)
+            raise JneError(rc, f"request {rid} not fetched")
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            self._L.jne_server_close(self._h)
+            self._h = None
+
+    def __enter__(self) -> "Server":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
 
 
 # --------------------------------------------------------------------------
