@@ -159,18 +159,15 @@ def run_gpu(args, rank: int, world: int) -> None:
     seed0 = 1 + rank * R  # disjoint seed ranges per replica
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
+    # requests alternate between two caller streams, so the finalize of one
+    # request (on the engine's second stream) overlaps the next accumulation
+    streams = [stream, torch.cuda.Stream()]
     outs = {m: torch.empty((R, k_of(m)), dtype=torch.float64, device="cuda") for m in MODELS}
 
-    def step_device(prec, lat=None):
-        for m in MODELS:
-            if lat is not None:
-                e0 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            eng.eigs_seeded_device(m, DIM, STEPS, seed0, R, outs[m].data_ptr(), precision=prec, stream=sptr)
-            if lat is not None:
-                e1 = torch.cuda.Event(enable_timing=True)
-                e1.record(stream)
-                lat.append((e0, e1))
+    def step_device(prec):
+        for j, m in enumerate(MODELS):
+            st = streams[j % 2]
+            eng.eigs_seeded_device(m, DIM, STEPS, seed0, R, outs[m].data_ptr(), precision=prec, stream=st.cuda_stream)
 
     def barrier():
         if dist is not None:
@@ -188,26 +185,47 @@ def run_gpu(args, rank: int, world: int) -> None:
     for _ in range(args.warmup):
         step_device(jne.PREC_MIXED)
     barrier()
-    lat = []
+    step_ms = []
     eng.profile(True)  # per-kernel CUDA events on the launching stream
     eng.profile_read(reset=True)
     with ClockSampler(local) as clk:
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
+        streams[1].wait_stream(stream)
+        marks = []
         for _ in range(args.steps):
-            step_device(jne.PREC_MIXED, lat)
+            step_device(jne.PREC_MIXED)
+            stream.wait_stream(streams[1])
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            streams[1].wait_stream(stream)
+            marks.append(e)
         ev1.record(stream)
         barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1))
+    prev = ev0
+    for e in marks:
+        step_ms.append(prev.elapsed_time(e))
+        prev = e
     eng.sync()  # device status of the asynchronous calls
     prof = eng.profile_read(reset=True)
     eng.profile(False)
     runs_per_step = R * len(MODELS) * world
     value = runs_per_step * args.steps / (ms * 1e-3)
-    lat_ms = sorted(a.elapsed_time(b) for a, b in lat)
-    p50 = float(np.percentile(lat_ms, 50))
-    p99 = float(np.percentile(lat_ms, 99))
+    # latency of one request issued alone (device time, synchronous)
+    iso = []
+    for m in MODELS:
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.eigs_seeded_device(m, DIM, STEPS, seed0, R, outs[m].data_ptr(), precision=jne.PREC_MIXED, stream=sptr)
+        b.record(stream)
+        b.synchronize()
+        iso.append(a.elapsed_time(b))
+    eng.sync()
+    p50 = float(np.percentile(iso, 50))
+    p99 = float(np.percentile(iso, 99))
 
     # ---- end to end through the host-memory C call (e2e) ----
     host = {m: np.empty((R, k_of(m))) for m in MODELS}
@@ -294,8 +312,10 @@ def run_gpu(args, rank: int, world: int) -> None:
                        "l2": "working set larger than L2: moment records of a 5-model step are "
                              f"{R * 294 * 8 * 5 / 1e9:.2f} GB; no inputs (increments generated in-kernel)",
                        "parallelism": f"replicas x{world} over disjoint seed ranges"},
-            "latency_ms": {"per_request_p50": p50, "per_request_p99": p99,
-                           "request": f"{R} runs of one model"},
+            "latency_ms": {"request_alone_p50": p50, "request_alone_p99": p99,
+                           "request": f"{R} runs of one model, issued alone",
+                           "step_p50": float(np.percentile(step_ms, 50)), "step_p99": float(np.percentile(step_ms, 99)),
+                           "step": "5 requests, one per model, pipelined"},
             "fp64_plain": {"value": fp64_value, "unit": UNIT, "runs_per_model": Rf,
                            "mixed_speedup": value / fp64_value},
             "mixed_error": {"vs": "plain FP64 kernel, identical seeds", "runs_per_model": ns, "per_model": err},
@@ -373,9 +393,11 @@ def bench_serving(jne, local: int, seconds: float, rate: float = 200.0, seed: in
                 if delay > 0:
                     time.sleep(delay)
                 ids.append(srv.submit(**r))
-            done = {}
+            done, t_wait = {}, time.perf_counter()
             while len(done) < len(ids):
-                for c in srv.wait(timeout_ms=120_000):
+                if time.perf_counter() - t_wait > 300:
+                    raise RuntimeError(f"serving: only {len(done)} of {len(ids)} requests finished")
+                for c in srv.wait(timeout_ms=5_000):
                     done[c.id] = c
             for i in ids:
                 srv.fetch(i)

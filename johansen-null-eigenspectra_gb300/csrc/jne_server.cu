@@ -39,6 +39,7 @@ struct Job {
   int64_t done = 0;         // runs whose iteration has completed
   double submit_s = 0, start_s = -1, finish_s = 0;
   int status = JNE_OK;
+  bool admitted = false;     // its output buffer counts against the budget
   bool writing = false;      // queued for or being written by the writer thread
   std::vector<double> host;  // results, once finished
 };
@@ -77,11 +78,12 @@ struct jne_server {
 
 namespace {
 
-// Device bytes the server may hold for outputs: the budget minus the records
-// of the two ragged launches in flight.
+// Device bytes the server may hold for outputs: half the budget less a small
+// margin; the records of the two ragged launches in flight take at most a
+// quarter each, and the request tables the margin.
 unsigned long long output_room(const jne_server* s) {
   const unsigned long long b = s->ctx->budget;
-  return b > b / 2 ? b - b / 2 : 0;
+  return b / 2 - b / 64;
 }
 
 void finish_job(jne_server* s, Job* j, int status) {
@@ -94,8 +96,11 @@ void finish_job(jne_server* s, Job* j, int status) {
   j->d_out = nullptr;
   j->finish_s = s->now();
   std::lock_guard<std::mutex> lk(s->mu);
-  s->ctx->in_use -= j->bytes;
-  s->admitted_bytes -= j->bytes;
+  if (j->admitted) {
+    s->ctx->in_use -= j->bytes;
+    s->admitted_bytes -= j->bytes;
+    j->admitted = false;
+  }
   s->finished[j->id] = j;
   s->completions.push_back({j->id, j->status, j->submit_s, j->start_s < 0 ? j->finish_s : j->start_s, j->finish_s,
                             j->req.n_runs});
@@ -162,11 +167,18 @@ void worker_loop(jne_server* s) {
           lk.lock();
           continue;
         }
-        if (s->admitted_bytes + j->bytes > output_room(s) || c->in_use + j->bytes > c->budget) break;
-        if (j->bytes && cudaMallocAsync((void**)&j->d_out, j->bytes, c->stream) != cudaSuccess) break;
+        if (s->admitted_bytes + j->bytes > output_room(s)) break;  // wait for running requests to finish
+        if (cudaMallocAsync((void**)&j->d_out, j->bytes, c->stream) != cudaSuccess) {
+          s->pending.pop_front();
+          lk.unlock();
+          finish_job(s, j, JNE_ERR_CUDA);
+          lk.lock();
+          continue;
+        }
         s->pending.pop_front();
         s->admitted_bytes += j->bytes;
         c->in_use += j->bytes;
+        j->admitted = true;
         j->start_s = -1;
         s->active.push_back(j);
       }

@@ -22,10 +22,11 @@ MIX = [
 ]
 
 
-def _collect(srv, n):
-    done = {}
+def _collect(srv, n, limit_s=120.0):
+    done, t0 = {}, time.monotonic()
     while len(done) < n:
-        for c in srv.wait(timeout_ms=60_000):
+        assert time.monotonic() - t0 < limit_s, f"only {len(done)} of {n} requests finished"
+        for c in srv.wait(timeout_ms=5_000):
             done[c.id] = c
     return done
 
