@@ -104,13 +104,23 @@ def measured_peaks():
         return {}
 
 
-def cpu_sample(oracle, runs_per_model: int, threads: int):
+def cpu_sample(oracle, runs_per_model: int, threads: int, seed_first: int = 1):
     """Oracle (dense restatement) on `threads` host threads; returns runs/s."""
     t0 = time.perf_counter()
     for m in MODELS:
-        oracle.c_eigs_seeded(m, DIM, STEPS, 1, runs_per_model, n_threads=threads)
+        oracle.c_eigs_seeded(m, DIM, STEPS, seed_first, runs_per_model, n_threads=threads)
     dt = time.perf_counter() - t0
     return len(MODELS) * runs_per_model / dt, dt
+
+
+def cpu_sample_for(oracle, seconds: float, threads: int, batch: int):
+    """Repeats `batch` runs per model over fresh seeds until `seconds` of wall
+    time have passed; returns (runs/s, runs per model, seconds)."""
+    done, total, seed = 0, 0.0, 1
+    while total < seconds:
+        _, dt = cpu_sample(oracle, batch, threads, seed)
+        done, total, seed = done + batch, total + dt, seed + batch
+    return len(MODELS) * done / total, done, total
 
 
 def run_reference(args, rank: int, world: int) -> None:
@@ -120,7 +130,7 @@ def run_reference(args, rank: int, world: int) -> None:
 
     oracle = entry.load_oracle()
     threads = os.cpu_count() or 1
-    per_model = args.cpu_runs or max(threads, 4 * threads)
+    per_model = args.cpu_runs or 128 * threads  # ~3 s per step on 16 Neoverse-V2 cores
     for _ in range(args.warmup):
         cpu_sample(oracle, max(threads, per_model // 4), threads)
     times = []
@@ -285,9 +295,12 @@ def run_gpu(args, rank: int, world: int) -> None:
             "kernel": "k_accum_mixed<12,false>", "peak_source": "measured bf16_tflops (burst)" if bf16 else "none",
             "flops_per_run": W}
     normals_rate = DIM * STEPS * R / (mean_acc_ms * 1e-3)
-    issue = {"normals_per_s": normals_rate, "peak_normals_per_s": args.rng_peak,
-             "frac": normals_rate / args.rng_peak,
-             "note": "Philox4x32-10 + Box-Muller rate measured by a standalone throughput kernel on GB300"}
+    rates = eng.probe_rates()
+    rng_peak = args.rng_peak or rates["normals_per_s"]
+    issue = {"normals_per_s": normals_rate, "peak_normals_per_s": rng_peak,
+             "frac": normals_rate / rng_peak, "probe_rates": rates,
+             "note": "normals/s the accumulation kernel draws vs the rate of the same Philox4x32-10 + "
+                     "Box-Muller device code alone (jne_probe_rates, measured in this run)"}
 
     ragged = bench_ragged60(jne, torch, local, args.ragged_steps) if args.ragged_steps > 0 and rank == 0 else None
     serving = bench_serving(jne, local, args.serve_seconds) if args.serve_seconds > 0 and rank == 0 else None
@@ -296,8 +309,11 @@ def run_gpu(args, rank: int, world: int) -> None:
     if rank == 0 and args.cpu_runs != 0:
         oracle = entry.load_oracle()
         threads = os.cpu_count() or 1
-        per = args.cpu_runs or 4 * threads
-        v, dt = cpu_sample(oracle, per, threads)
+        if args.cpu_runs:
+            per = args.cpu_runs
+            v, dt = cpu_sample(oracle, per, threads)
+        else:
+            v, per, dt = cpu_sample_for(oracle, args.cpu_seconds, threads, 16 * threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{per} runs x 5 models (seeds 1..{per}), dim {DIM}, T {STEPS}, {dt:.1f} s wall"}
 
@@ -421,11 +437,13 @@ def main() -> None:
     ap.add_argument("--fp64-runs", type=int, default=20_000)
     ap.add_argument("--err-runs", type=int, default=2_000)
     ap.add_argument("--cpu-runs", type=int, default=None, help="CPU sample runs per model (0 = skip)")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length without --cpu-runs")
     ap.add_argument("--chunk", type=int, default=0, help="steps per FP32 chunk (0: adaptive, 256 at T=10k)")
     ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per accumulation launch")
     ap.add_argument("--ragged-steps", type=int, default=2, help="timed replays of the ragged 60-pair plan (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="Poisson arrival window of the serving run (0: skip)")
-    ap.add_argument("--rng-peak", type=float, default=1.016e12, help="measured Philox+Box-Muller normals/s")
+    ap.add_argument("--rng-peak", type=float, default=None,
+                    help="Philox+Box-Muller normals/s (default: measured live by jne_probe_rates)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -23,7 +23,7 @@
  *   jne_dat_*                  src/data_storage/{writer,reader,uleb128}.rs
  *   jne_simulation_*           src/data_storage/simulation.rs:25-122 and
  *                              parallel_compute.rs:150-232
- *   jne_percentiles            src/simulation_analyzers.rs:4-81
+ *   jne_percentiles(_device)   src/simulation_analyzers.rs:4-81
  */
 #ifndef JNE_H
 #define JNE_H
@@ -192,6 +192,19 @@ int jne_server_close(jne_server* server);
 int jne_profile(jne_context* ctx, int enable);
 int jne_profile_read(jne_context* ctx, double* ms, long long* launches, int reset);
 
+/* Measures, on ctx's device, the rates that bound the accumulation kernels:
+ * rates[0] normals/s drawn by the kernels' own Philox4x32-10 + Box-Muller code,
+ * rates[1] FP64 FMA flop/s, rates[2] TF32 mma.sync flop/s, rates[3] FP32 FMA
+ * flop/s (JNE_RATE_*).  Each is one ~10-50 ms launch over 8 blocks per SM,
+ * timed with CUDA events after a warm-up launch.  Diagnostic: no counterpart in
+ * the reference. */
+#define JNE_RATE_NORMALS 0
+#define JNE_RATE_DFMA 1
+#define JNE_RATE_MMA_TF32 2
+#define JNE_RATE_FFMA 3
+#define JNE_RATE_KINDS 4
+int jne_probe_rates(jne_context* ctx, double* rates);
+
 /* The increments the seeded path draws for these runs, scaled by sqrt(1/steps):
  * dB_out receives n_runs consecutive dim x steps column-major matrices (may be
  * null); words_out receives the raw Philox words, n_runs x steps x
@@ -244,8 +257,19 @@ int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int di
 
 /* Percentiles (simulation_analyzers.rs:4-81) of the trace (stat 0) or the
  * largest eigenvalue (stat 1) of n records of k eigenvalues: linear
- * interpolation at rank p * (n - 1) of the sorted statistic; NaN when n == 0. */
+ * interpolation at rank p * (n - 1) of the sorted statistic; NaN when n == 0.
+ * Every p must lie in [0, 1] (JNE_ERR_ARG); a NaN statistic gives
+ * JNE_ERR_NUMERIC (the reference's sort panics on NaN). */
 int jne_percentiles(const double* eigs, int64_t n, int k, int stat, const double* ps, int np, double* out);
+
+/* The same percentiles of eigenvalues in device memory (n x k, run-major), by
+ * a radix select on the device instead of a sort; bit-identical to
+ * jne_percentiles.  Work the caller enqueued on `stream` (null: the legacy
+ * default stream) before the call is waited for; ps / out are host memory and
+ * the call returns when `out` is written.  Scratch: 8 bytes per run within the
+ * context's budget.  Replaces calculate_percentiles, simulation_analyzers.rs:42-65. */
+int jne_percentiles_device(jne_context* ctx, const double* eigs_device, int64_t n, int k, int stat, const double* ps,
+                           int np, double* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -30,14 +30,15 @@ MAX_DIM = 12
 EXPORTS = (
     "jne_version", "jne_eigen_count", "jne_open", "jne_close", "jne_last_error", "jne_set_chunk",
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
-    "jne_export_increments", "jne_profile", "jne_profile_read", "jne_sync",
+    "jne_export_increments", "jne_profile", "jne_profile_read", "jne_probe_rates", "jne_sync",
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
-    "jne_simulation_filename", "jne_simulation_run", "jne_percentiles",
+    "jne_simulation_filename", "jne_simulation_run", "jne_percentiles", "jne_percentiles_device",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
     "jne_run_batch", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
     "jne_server_open", "jne_server_submit", "jne_server_wait", "jne_server_fetch", "jne_server_close",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
+RATE_KINDS = ("normals_per_s", "dfma_flops", "mma_tf32_flops", "ffma_flops")
 
 
 class Request(ctypes.Structure):
@@ -162,6 +163,8 @@ def lib() -> ctypes.CDLL:
         L.jne_server_close.argtypes = [vp]
         L.jne_profile.argtypes = [vp, c_int]
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
+        L.jne_probe_rates.argtypes = [vp, dp]
+        L.jne_percentiles_device.argtypes = [vp, vp, c_i64, c_int, c_int, dp, c_int, dp, vp]
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
         L.jne_dat_open.argtypes = [ctypes.c_char_p, c_int, c_int, c_u32, ctypes.POINTER(vp), i64p]
         L.jne_dat_append.argtypes = [vp, u32p, dp, c_i64, c_int]
@@ -228,6 +231,24 @@ class Engine:
         n = (ctypes.c_longlong * 4)()
         self._check(self._L.jne_profile_read(self._h, _dp(ms), n, int(reset)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(KERNEL_KINDS)}
+
+    def percentiles_device(self, eigs_ptr: int, n: int, k: int, stat: str, ps: Sequence[float],
+                           stream: int = 0) -> List[float]:
+        """Percentiles of the trace ('trace') or largest eigenvalue ('maxeig') of n
+        runs of k eigenvalues at device address eigs_ptr, selected on the device."""
+        p = np.ascontiguousarray(ps, dtype=np.float64)
+        out = np.empty(len(p))
+        self._check(self._L.jne_percentiles_device(self._h, ctypes.c_void_p(eigs_ptr), int(n), int(k),
+                                                    0 if stat == "trace" else 1, _dp(p), len(p), _dp(out),
+                                                    ctypes.c_void_p(stream)))
+        return out.tolist()
+
+    def probe_rates(self) -> Dict[str, float]:
+        """Measured pipe rates of this GPU: normals/s of the kernels' RNG code, and
+        FP64-FMA, TF32-mma and FP32-FMA flop/s."""
+        r = np.zeros(len(RATE_KINDS))
+        self._check(self._L.jne_probe_rates(self._h, _dp(r)))
+        return {k: float(r[i]) for i, k in enumerate(RATE_KINDS)}
 
     def eigs_from_increments(self, model: int, dB: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:
         """dB: (n_runs, steps, dim) -- each run's dim x steps increment matrix, column-major."""

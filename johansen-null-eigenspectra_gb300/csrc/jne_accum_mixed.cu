@@ -41,12 +41,23 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// d = A B (no accumulator input): starts a tile's hi*hi sum without zeroing it first.
+__device__ __forceinline__ void mma_tf32_first(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%10,%10,%10,%10};\n"
+      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1), "f"(0.0f));
+}
+
 // A B with A, B given as float values, on the TF32 split: the hi*hi product
-// goes to `hh`, the two cross products to `x`.  The tensor core's FP32
+// goes to `hh` (overwritten when FIRST), the two cross products to `x`.  The tensor core's FP32
 // accumulation truncates, so its error is biased and grows with the number of
 // additions into one accumulator: keeping the (2^11 times smaller) cross terms
 // apart and emptying `hh` after every tile keeps that bias ~10x below a single
 // accumulator per chunk.
+template <bool FIRST>
 __device__ __forceinline__ void mma_split(float (&hh)[4], float (&x)[4], float a0, float a1, float a2, float a3,
                                           float b0, float b1) {
   const uint32_t ah0 = tf32_hi(a0), ah1 = tf32_hi(a1), ah2 = tf32_hi(a2), ah3 = tf32_hi(a3);
@@ -56,7 +67,10 @@ __device__ __forceinline__ void mma_split(float (&hh)[4], float (&x)[4], float a
   const uint32_t bl0 = __float_as_uint(b0 - __uint_as_float(bh0)), bl1 = __float_as_uint(b1 - __uint_as_float(bh1));
   mma_tf32(x, al0, al1, al2, al3, bh0, bh1);
   mma_tf32(x, ah0, ah1, ah2, ah3, bl0, bl1);
-  mma_tf32(hh, ah0, ah1, ah2, ah3, bh0, bh1);
+  if (FIRST)
+    mma_tf32_first(hh, ah0, ah1, ah2, ah3, bh0, bh1);
+  else
+    mma_tf32(hh, ah0, ah1, ah2, ah3, bh0, bh1);
 }
 
 // Two-sum carry update: (hi, lo) += t.
@@ -74,16 +88,23 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float t) {
 template <int DIM, bool FULL>
 __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, int tloc, int nvalid,
                                           float invL, const float (&cA)[4], const float (&cB)[4],
-                                          float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[4][4],
-                                          float (&accx)[4][4]) {
+                                          float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[3][4],
+                                          float (&accx)[3][4]) {
+  // zA: increments of row g; zB: of row 8 + (g & 3) -- the walk of row g + 8
+  // for g < 4, the B operand of Gram block 1 for g >= 4 (rows >= DIM are zero)
   float zA[8], zB[8];
   {
     const float4 p0 = *reinterpret_cast<const float4*>(&zs[g][8 * q]);
     const float4 p1 = *reinterpret_cast<const float4*>(&zs[g][8 * q + 4]);
-    const float4 r0 = *reinterpret_cast<const float4*>(&zs[g + 8][8 * q]);
-    const float4 r1 = *reinterpret_cast<const float4*>(&zs[g + 8][8 * q + 4]);
     zA[0] = p0.x; zA[1] = p0.y; zA[2] = p0.z; zA[3] = p0.w; zA[4] = p1.x; zA[5] = p1.y; zA[6] = p1.z; zA[7] = p1.w;
-    zB[0] = r0.x; zB[1] = r0.y; zB[2] = r0.z; zB[3] = r0.w; zB[4] = r1.x; zB[5] = r1.y; zB[6] = r1.z; zB[7] = r1.w;
+    if (DIM > 8) {
+      const float4 r0 = *reinterpret_cast<const float4*>(&zs[8 + (g & 3)][8 * q]);
+      const float4 r1 = *reinterpret_cast<const float4*>(&zs[8 + (g & 3)][8 * q + 4]);
+      zB[0] = r0.x; zB[1] = r0.y; zB[2] = r0.z; zB[3] = r0.w; zB[4] = r1.x; zB[5] = r1.y; zB[6] = r1.z; zB[7] = r1.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) zB[j] = 0.f;
+    }
   }
   // lane totals and the exclusive scan over the 4 lanes of the group
   float tA = ((zA[0] + zA[1]) + (zA[2] + zA[3])) + ((zA[4] + zA[5]) + (zA[6] + zA[7]));
@@ -103,12 +124,13 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   // G rows rA = g and rB = g + 8 at the lane's 8 steps
   float GA[8], GB[8];
   float pA = cloA + eA, pB = cloB + eB;  // tile-local walk (+ carry low word)
+  const float u0 = (float)tloc * invL;
 #pragma unroll
   for (int j = 0; j < 8; j++) {
     const float bA = chiA + pA, bB = chiB + pB;
     pA += zA[j];
     pB += zB[j];
-    const float u = (float)(tloc + j) * invL;
+    const float u = fmaf((float)j, invL, u0);
     if (DIM >= 8) {
       GA[j] = bA;
     } else {
@@ -122,22 +144,31 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   ff_add(chiA, cloA, tileA);
   ff_add(chiB, cloB, tileB);
 
-  float hh[4][4];
+  // Gram blocks (16 G rows x 8 columns each):
+  //   0: G x walk 0..7;  1 (DIM > 8): G x [walk 8..11 | z 8..11];  2: G x z 0..7.
+  // Block 1's column g is walk row 8 + g (held as GB by lane g < 4) or z row
+  // 8 + g - 4 (held as zB by lane g >= 4).  Products of the basis rows with
+  // themselves are known in closed form and never formed.
+  float BB[8];
 #pragma unroll
-  for (int n = 0; n < 4; n++)
+  for (int j = 0; j < 8; j++) BB[j] = g < 4 ? GB[j] : zB[j];
+  float hh[3][4];
+  if (DIM <= 8)
 #pragma unroll
-    for (int r = 0; r < 4; r++) hh[n][r] = 0.f;
+    for (int r = 0; r < 4; r++) hh[1][r] = 0.f;
+  mma_split<true>(hh[0], accx[0], GA[0], GB[0], GA[1], GB[1], GA[0], GA[1]);
+  if (DIM > 8) mma_split<true>(hh[1], accx[1], GA[0], GB[0], GA[1], GB[1], BB[0], BB[1]);
+  mma_split<true>(hh[2], accx[2], GA[0], GB[0], GA[1], GB[1], zA[0], zA[1]);
 #pragma unroll
-  for (int s = 0; s < 4; s++) {
+  for (int s = 1; s < 4; s++) {
     const int j0 = 2 * s, j1 = 2 * s + 1;
-    mma_split(hh[0], accx[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
-    if (DIM + 3 > 8) mma_split(hh[1], accx[1], GA[j0], GB[j0], GA[j1], GB[j1], GB[j0], GB[j1]);
-    mma_split(hh[2], accx[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
-    if (DIM > 8) mma_split(hh[3], accx[3], GA[j0], GB[j0], GA[j1], GB[j1], zB[j0], zB[j1]);
+    mma_split<false>(hh[0], accx[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
+    if (DIM > 8) mma_split<false>(hh[1], accx[1], GA[j0], GB[j0], GA[j1], GB[j1], BB[j0], BB[j1]);
+    mma_split<false>(hh[2], accx[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
   }
   // empty the tile's hi*hi accumulator into the chunk sum (round to nearest)
 #pragma unroll
-  for (int n = 0; n < 4; n++)
+  for (int n = 0; n < 3; n++)
 #pragma unroll
     for (int r = 0; r < 4; r++) acc[n][r] = __fadd_rn(acc[n][r], hh[n][r]);
 }
@@ -220,9 +251,9 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
 
   for (int c0 = 0; c0 < T; c0 += L) {
     const int Lc = min(L, T - c0);
-    float acc[4][4], accx[4][4];  // chunk sums: hi*hi (emptied per tile) and cross terms
+    float acc[3][4], accx[3][4];  // chunk sums: hi*hi (emptied per tile) and cross terms
 #pragma unroll
-    for (int n = 0; n < 4; n++)
+    for (int n = 0; n < 3; n++)
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         acc[n][r] = 0.f;
@@ -258,13 +289,16 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
       __syncwarp();
     }
 
-    // ---- chunk end: stage the local Gram and the chunk totals ----
+    // ---- chunk end: stage the local Gram (cm[row][col], col < 16: walk column,
+    //      16 + f: increment f) and the chunk totals ----
 #pragma unroll
-    for (int n = 0; n < 4; n++) {
-      cm[g][8 * n + 2 * q] = acc[n][0] + accx[n][0];
-      cm[g][8 * n + 2 * q + 1] = acc[n][1] + accx[n][1];
-      cm[g + 8][8 * n + 2 * q] = acc[n][2] + accx[n][2];
-      cm[g + 8][8 * n + 2 * q + 1] = acc[n][3] + accx[n][3];
+    for (int n = 0; n < 3; n++) {
+      if (n == 1 && DIM <= 8) continue;
+      const int col = n == 0 ? 2 * q : n == 2 ? 16 + 2 * q : (q < 2 ? 8 + 2 * q : 20 + 2 * q);
+      cm[g][col] = acc[n][0] + accx[n][0];
+      cm[g][col + 1] = acc[n][1] + accx[n][1];
+      cm[g + 8][col] = acc[n][2] + accx[n][2];
+      cm[g + 8][col + 1] = acc[n][3] + accx[n][3];
     }
     if (q == 0) {
       if (g < d) tz[g] = (double)chiA + (double)cloA;
@@ -299,45 +333,32 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
       cuuz[f] = Suuz - 2.0f * ub * Suz + ub * ub * tzf - qbar * tzf;       // sum ((u-ubar)^2 - qbar) z
     }
     __syncwarp();
-    // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy
-    for (int e = lane; e < NREC; e += 32) {
-      double v64;
-      float v32;
-      if (e < NMWW) {
-        const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
-        v64 = lm[p] * mm[r];
-        v32 = cm[p][r] - sbf[p] * sbf[r] * invLcf;
-      } else if (e < NMWW + NMW) {
-        const int t = e - NMWW, pp = t / d, r = t - pp * d;
-        if (pp == 0) {
-          v64 = lm[r];
-          v32 = 0.f;
-        } else if (pp == 1) {
-          v64 = ct.ybar * lm[r];
-          v32 = hf * cub[r];
-        } else {
-          v64 = ct.y2bar * lm[r];
-          v32 = 2.0f * ybf * hf * cub[r] + hf * hf * cuub[r];
-        }
-      } else if (e < NMWW + NMW + NNZW) {
-        const int t = e - NMWW - NMW, za = t / d, wb = t - za * d;
-        v64 = tz[za] * mm[wb];
-        v32 = cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf;
-      } else if (e < NMWW + NMW + NNZW + d) {
-        v64 = 0.0;  // Nz1: the walk's end point, written from wc
-        v32 = 0.f;
-      } else {
-        const int t = e - NMWW - NMW - NNZW - d, pp = 1 + t / d, za = t - (pp - 1) * d;
-        if (pp == 1) {
-          v64 = ct.ybar * tz[za];
-          v32 = hf * cuz[za];
-        } else {
-          v64 = ct.y2bar * tz[za];
-          v32 = 2.0f * ybf * hf * cuz[za] + hf * hf * cuuz[za];
-        }
-      }
-      rec[e] += v64;
-      ff_add(rech[e], recl[e], v32);
+    // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy.
+    // One loop per slot kind, so the lanes of an iteration take one path.
+    const float c1y = hf, c2y = 2.0f * ybf * hf, c2yy = hf * hf;  // y and y^2 coefficients
+    for (int e = lane; e < NMWW; e += 32) {
+      const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
+      rec[e] += lm[p] * mm[r];
+      ff_add(rech[e], recl[e], cm[p][r] - sbf[p] * sbf[r] * invLcf);
+    }
+    for (int t = lane; t < NMW; t += 32) {
+      const int pp = t / d, r = t - pp * d, e = NMWW + t;
+      const double w64 = pp == 0 ? 1.0 : pp == 1 ? ct.ybar : ct.y2bar;
+      const float a1 = pp == 0 ? 0.f : pp == 1 ? c1y : c2y, a2 = pp == 2 ? c2yy : 0.f;
+      rec[e] += w64 * lm[r];
+      ff_add(rech[e], recl[e], a1 * cub[r] + a2 * cuub[r]);
+    }
+    for (int t = lane; t < NNZW; t += 32) {
+      const int za = t / d, wb = t - za * d, e = NMWW + NMW + t;
+      rec[e] += tz[za] * mm[wb];
+      ff_add(rech[e], recl[e], cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf);
+    }
+    for (int t = lane; t < 2 * d; t += 32) {
+      const int pp = t / d, za = t - pp * d, e = NMWW + NMW + NNZW + d + t;
+      const double w64 = pp == 0 ? ct.ybar : ct.y2bar;
+      const float a1 = pp == 0 ? c1y : c2y, a2 = pp == 0 ? 0.f : c2yy;
+      rec[e] += w64 * tz[za];
+      ff_add(rech[e], recl[e], a1 * cuz[za] + a2 * cuuz[za]);
     }
     __syncwarp();
     if (lane < d) wc[lane] += tz[lane];
@@ -353,14 +374,27 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
 }
 
 // One request: every warp strides over its runs.
+// The round keys arrive as a kernel parameter (computed on the host): the
+// Philox rounds read them from the parameter bank instead of holding 20
+// registers.
 template <int DIM, bool EXT>
-__global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4) k_accum_mixed(const jne_accum_args a) {
+__global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
+    k_accum_mixed(const __grid_constant__ jne_accum_args a, const __grid_constant__ jne_round_keys rk) {
   __shared__ WarpSmem sm_all[kMixWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
   const int nwarps = gridDim.x * kMixWarps;
-  for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps)
-    accum_run<DIM, EXT>(a, run, sm_all[wib], rk, lane);
+  if (a.next_run == nullptr) {
+    for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps)
+      accum_run<DIM, EXT>(a, run, sm_all[wib], rk, lane);
+    return;
+  }
+  // first run by warp index, then the next free one from the counter
+  for (long long run = blockIdx.x * kMixWarps + wib; run < a.n_runs;) {
+    accum_run<DIM, EXT>(a, (int)run, sm_all[wib], rk, lane);
+    unsigned long long item = 0;
+    if (lane == 0) item = atomicAdd(a.next_run, 1ull);
+    run = nwarps + (long long)__shfl_sync(0xffffffffu, item, 0);
+  }
 }
 
 // A ragged batch of requests (any dims, step counts and sizes) in one
@@ -416,12 +450,13 @@ int resident_grid(K kernel, int threads, size_t shm, int sms, long long n_runs, 
 template <int DIM>
 cudaError_t launch_dim(const jne_accum_args& a, int sms, cudaStream_t st) {
   const int threads = kMixWarps * JNE_WARP;
+  const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
   if (a.ext) {
     auto k = k_accum_mixed<DIM, true>;
-    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a);
+    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk);
   } else {
     auto k = k_accum_mixed<DIM, false>;
-    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a);
+    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk);
   }
   return cudaGetLastError();
 }

@@ -43,11 +43,12 @@ int jne_open(int device, unsigned long long mem_budget_bytes, jne_context** out)
   if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, sizeof(unsigned int));
   // the asynchronous paths only clear the status in jne_sync: start from zero
   if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_next_run, sizeof(unsigned long long));
   if (e != cudaSuccess) {
     jne_close(c);
     return JNE_ERR_CUDA;
   }
-  c->in_use = sizeof(unsigned int);
+  c->in_use = sizeof(unsigned int) + sizeof(unsigned long long);
   *out = c;
   return JNE_OK;
 }
@@ -66,6 +67,8 @@ void jne_close(jne_context* c) {
   cudaFree(c->d_ent);
   cudaFree(c->d_ctab);
   cudaFree(c->d_status);
+  cudaFree(c->d_next_run);
+  cudaFree(c->d_qscratch);
   if (c->ev_in) cudaEventDestroy(c->ev_in);
   for (int i = 0; i < 2; i++) {
     cudaFree(c->d_reqs[i]);

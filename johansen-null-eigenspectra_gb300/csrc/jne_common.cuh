@@ -150,6 +150,8 @@ struct jne_accum_args {
   double* mom;               // moment records, SoA
   long long mom_ld;          // leading dimension (>= n_runs)
   unsigned int* status;      // device status word (bit flags), may be null
+  unsigned long long* next_run;  // mixed kernel: zeroed work counter for dynamic run
+                                 // assignment, or null for a fixed stride per warp
 };
 
 // Status bits a kernel may raise (never a trap).

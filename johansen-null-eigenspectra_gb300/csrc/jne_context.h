@@ -32,6 +32,9 @@ struct jne_context {
   int4* d_ent = nullptr;
   size_t ent_cap = 0;
   unsigned int* d_status = nullptr;
+  unsigned long long* d_next_run = nullptr;  // work counter of single-request mixed launches
+  unsigned long long* d_qscratch = nullptr;  // percentile analyzer: keys, ranks, histograms
+  size_t qscratch_cap = 0;
   std::string err;
   // asynchronous device path: two record buffers, finalize on a second stream
   cudaStream_t fin_stream = nullptr;
@@ -264,6 +267,11 @@ inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t ke
     c->ctab_chunk = a.chunk;
     }
     a.chunk_tab = c->d_ctab;
+    // warps take runs from a counter, so blocks that start late (behind a
+    // concurrent finalize) take fewer runs instead of leaving a tail
+    e = cudaMemsetAsync(c->d_next_run, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "work counter reset");
+    a.next_run = c->d_next_run;
     ProfScope ps(c, JNE_KERNEL_ACCUM_MIXED, st);
     e = jne_launch_accum_mixed(a, c->sms, st);
   }

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_set>
 #include <vector>
 
@@ -110,15 +111,18 @@ int read_file(const char* path, std::vector<unsigned char>* buf) {
   return JNE_OK;
 }
 
+// A file's header fields and record index: the seed of every record and the
+// byte offset of its first eigenvalue (the values are decoded separately).
 struct Parsed {
   int model = 0, dim = 0, k = 0;
   uint32_t steps = 0;
   std::vector<uint32_t> seeds;
-  std::vector<double> eigs;
+  std::vector<size_t> vals;
 };
 
-// reader.rs:23-216.  Fast path when the EOF trailer is present, scan otherwise.
-int parse(const std::vector<unsigned char>& b, Parsed* out, bool want_records) {
+// reader.rs:23-216.  Fast path when the EOF trailer is present (its record
+// count sizes the index up front), scan otherwise.
+int parse(const std::vector<unsigned char>& b, Parsed* out) {
   if (b.size() < 12 || std::memcmp(b.data(), kMagic, 12) != 0)
     return dat_fail(JNE_ERR_FORMAT, "File format error: magic header mismatch");
   if (b.size() < kHeader) return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
@@ -132,6 +136,11 @@ int parse(const std::vector<unsigned char>& b, Parsed* out, bool want_records) {
   if (std::memcmp(&b[n - kTrailer], kEof, 8) == 0) {
     const uint64_t total = get_u64(&b[n - 9]);
     const int per = b[n - 1];
+    // every record takes at least 2 + 8 per bytes: a count beyond that is corrupt
+    if (total > (n - kHeader - kTrailer) / (2 + 8 * (size_t)std::max(per, 1)))
+      return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
+    out->seeds.reserve((size_t)total);
+    out->vals.reserve((size_t)total);
     for (uint64_t r = 0; r < total; r++) {
       uint32_t seed;
       size_t used;
@@ -145,12 +154,8 @@ int parse(const std::vector<unsigned char>& b, Parsed* out, bool want_records) {
         return dat_fail(JNE_ERR_FORMAT, "Eigenvalue count mismatch: expected " + std::to_string(per) + ", actual " +
                                             std::to_string(cnt));
       if (pos + 8 * (size_t)cnt > n) return dat_fail(JNE_ERR_IO, "failed to fill whole buffer");
-      if (want_records) {
-        out->seeds.push_back(seed);
-        for (int j = 0; j < cnt; j++) out->eigs.push_back(get_f64(&b[pos + 8 * j]));
-      } else {
-        out->seeds.push_back(seed);
-      }
+      out->seeds.push_back(seed);
+      out->vals.push_back(pos);
       pos += 8 * (size_t)cnt;
     }
     out->k = per;
@@ -172,12 +177,29 @@ int parse(const std::vector<unsigned char>& b, Parsed* out, bool want_records) {
     k = cnt;
     pos += used + 1;
     out->seeds.push_back(seed);
-    if (want_records)
-      for (int j = 0; j < cnt; j++) out->eigs.push_back(get_f64(&b[pos + 8 * j]));
+    out->vals.push_back(pos);
     pos += 8 * (size_t)cnt;
   }
   out->k = k < 0 ? 0 : k;
   return JNE_OK;
+}
+
+// The records' eigenvalues (little-endian f64) into eigs (n x k), records
+// split across host threads.
+void decode_values(const std::vector<unsigned char>& b, const Parsed& p, double* eigs) {
+  const size_t n = p.vals.size(), k = (size_t)p.k;
+  auto work = [&](size_t lo, size_t hi) {
+    for (size_t r = lo; r < hi; r++) {
+      const unsigned char* src = &b[p.vals[r]];
+      for (size_t j = 0; j < k; j++) eigs[r * k + j] = get_f64(src + 8 * j);
+    }
+  };
+  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>(std::min<size_t>(hw, 16), n / 65536 + 1);
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < nt; t++) pool.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+  work(0, n / nt);
+  for (auto& th : pool) th.join();
 }
 
 int write_header(FILE* f, int model, int dim, uint32_t steps) {
@@ -233,7 +255,7 @@ int jne_dat_open(const char* path, int model, int dim, uint32_t steps, jne_dat_w
     std::vector<unsigned char> b;
     Parsed p;
     int rc = read_file(path, &b);
-    if (rc == JNE_OK) rc = parse(b, &p, false);
+    if (rc == JNE_OK) rc = parse(b, &p);
     if (rc == JNE_OK) {
       const char* what = nullptr;
       int have = 0, want = 0;
@@ -333,7 +355,7 @@ int jne_dat_read(const char* path, int* model, int* dim, uint32_t* steps, int64_
   if (rc) return rc;
   Parsed p;
   const bool want = seeds && eigs;
-  if ((rc = parse(b, &p, want))) return rc;
+  if ((rc = parse(b, &p))) return rc;
   if (model) *model = p.model;
   if (dim) *dim = p.dim;
   if (steps) *steps = p.steps;
@@ -342,7 +364,7 @@ int jne_dat_read(const char* path, int* model, int* dim, uint32_t* steps, int64_
   if (want) {
     if (cap < (int64_t)p.seeds.size()) return dat_fail(JNE_ERR_ARG, "buffer too small");
     std::copy(p.seeds.begin(), p.seeds.end(), seeds);
-    std::copy(p.eigs.begin(), p.eigs.end(), eigs);
+    decode_values(b, p, eigs);
   }
   return JNE_OK;
 }
@@ -373,7 +395,7 @@ int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int di
   if (file_exists(path)) {
     std::vector<unsigned char> b;
     Parsed p;
-    if (read_file(path, &b) == JNE_OK && parse(b, &p, false) == JNE_OK) {
+    if (read_file(path, &b) == JNE_OK && parse(b, &p) == JNE_OK) {
       if (p.model != model || p.dim != dim || p.steps != (uint32_t)steps) {
         if (!quiet) std::printf("WARNING: Existing file has incompatible parameters; recreating %s\n", path);
         std::remove(path);
@@ -419,15 +441,21 @@ int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int di
 }
 
 int jne_percentiles(const double* eigs, int64_t n, int k, int stat, const double* ps, int np, double* out) {
-  if ((n > 0 && !eigs) || (np > 0 && (!ps || !out)) || k < 1 || n < 0 || (stat != 0 && stat != 1))
+  if ((n > 0 && !eigs) || (np > 0 && (!ps || !out)) || k < 1 || n < 0 || np < 0 || (stat != 0 && stat != 1))
     return dat_fail(JNE_ERR_ARG, "bad percentile arguments");
+  for (int i = 0; i < np; i++)
+    if (!(ps[i] >= 0.0 && ps[i] <= 1.0)) return dat_fail(JNE_ERR_ARG, "percentiles must lie in [0, 1]");
   std::vector<double> v((size_t)n);
+  int64_t nans = 0;
   for (int64_t r = 0; r < n; r++) {  // Sum / Max aggregators, simulation_analyzers.rs:26-39
     const double* e = eigs + (size_t)r * k;
     double a = stat == 0 ? 0.0 : -1.7976931348623157e308;
-    for (int j = 0; j < k; j++) a = stat == 0 ? a + e[j] : std::max(a, e[j]);
+    for (int j = 0; j < k; j++) a = stat == 0 ? a + e[j] : std::fmax(a, e[j]);
+    nans += a != a;
     v[(size_t)r] = a;
   }
+  // the reference's sort (partial_cmp().unwrap(), simulation_analyzers.rs:60) panics on NaN
+  if (nans) return dat_fail(JNE_ERR_NUMERIC, std::to_string(nans) + " runs have a NaN aggregate (unordered)");
   std::sort(v.begin(), v.end());
   for (int i = 0; i < np; i++) {  // simulation_analyzers.rs:4-18
     if (n == 0) {

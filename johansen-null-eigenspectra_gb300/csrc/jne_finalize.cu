@@ -104,16 +104,21 @@ __device__ bool tridiagonal_ql(double* dg, double* eo, int n) {
       bool underflow = false;
       for (; i >= l; i--) {
         const double f = s * eo[i], b = c * eo[i];
-        r = hypot(f, g);
-        eo[i + 1] = r;
-        if (r == 0.0) {  // recover from underflow
+        // Givens rotation from one reciprocal square root (the moments keep
+        // f and g far from the overflow / underflow range hypot guards)
+        const double r2 = fma(f, f, g * g);
+        if (r2 == 0.0) {  // recover from underflow
+          eo[i + 1] = 0.0;
           dg[i + 1] -= p;
           eo[m] = 0.0;
           underflow = true;
           break;
         }
-        s = f / r;
-        c = g / r;
+        const double ir = rsqrt(r2);
+        r = r2 * ir;
+        eo[i + 1] = r;
+        s = f * ir;
+        c = g * ir;
         g = dg[i + 1] - p;
         r = (dg[i] - g) * s + 2.0 * c * b;
         p = s * r;
@@ -172,8 +177,9 @@ __device__ void finalize_run(const jne_finalize_args& f, int run) {
     for (int j = 0; j < k; j++) E[cc][j] = c.N(x[j], cc) - al[j] * n1 - be[j] * ny;
   }
 
-  // Cholesky S11 = L L' (lower triangle of S)
+  // Cholesky S11 = L L' (lower triangle of S); inv[j] = 1 / L[j][j]
   bool ok = true;
+  double inv[JNE_MAX_K];
   for (int j = 0; j < k && ok; j++) {
     for (int i = 0; i <= j; i++) {
       double s = S[j][i];
@@ -181,8 +187,9 @@ __device__ void finalize_run(const jne_finalize_args& f, int run) {
       if (i == j) {
         if (!(s > 0.0)) { ok = false; break; }
         S[j][j] = sqrt(s);
+        inv[j] = 1.0 / S[j][j];
       } else {
-        S[j][i] = s / S[i][i];
+        S[j][i] = s * inv[i];
       }
     }
   }
@@ -197,7 +204,7 @@ __device__ void finalize_run(const jne_finalize_args& f, int run) {
     for (int j = 0; j < k; j++) {
       double s = E[cc][j];
       for (int p = 0; p < j; p++) s -= S[j][p] * E[cc][p];
-      E[cc][j] = s / S[j][j];
+      E[cc][j] = s * inv[j];
     }
   // C = E'E into S (full storage)
   for (int p = 0; p < k; p++)

@@ -205,3 +205,11 @@ def test_distribution_matches_cpu_oracle(engine, oracle):
                     # Monte Carlo error of a quantile: ~ sqrt(p(1-p)/n) / density; compare in rank space
                     rank_b = np.searchsorted(b, qa) / n
                     assert abs(rank_b - p) < 5 * np.sqrt(p * (1 - p) / n) + 2.0 / n, (model, p, qa, qb)
+
+
+def test_probe_rates_are_measured(engine):
+    r = engine.probe_rates()
+    assert set(r) == {"normals_per_s", "dfma_flops", "mma_tf32_flops", "ffma_flops"}
+    assert 1e10 < r["normals_per_s"] < 1e14
+    assert 1e11 < r["dfma_flops"] < r["ffma_flops"]
+    assert 1e12 < r["mma_tf32_flops"] < 1e16

@@ -146,3 +146,37 @@ def test_simulation_filenames(jne, tmp):  # filename_consistency.rs, simulation_
     a = jne.EigenvalueSimulation(0, 5, 999, 100, data_dir=tmp).get_filename()
     b = jne.EigenvalueSimulation(0, 5, 999, 500, data_dir=tmp).get_filename()
     assert a == b and os.path.basename(a) == "eigenvalues_model0_dim5_steps999.dat"
+
+
+def test_percentile_arguments_and_nan(jne):
+    eigs = np.array([[3.0, 1.0], [2.0, 0.5]])
+    with pytest.raises(jne.DatError):
+        jne.percentiles(eigs, "trace", [1.5])   # the reference indexes past the end
+    with pytest.raises(jne.DatError):
+        jne.percentiles(eigs, "trace", [-0.1])
+    bad = eigs.copy()
+    bad[1, 0] = np.nan                            # the reference's sort panics on NaN
+    with pytest.raises(jne.DatError) as ei:
+        jne.percentiles(bad, "trace", [0.5])
+    assert ei.value.code == jne.JNE_ERR_NUMERIC
+    # the Max aggregator folds with f64::max, which skips NaN
+    assert jne.percentiles(bad, "maxeig", [0.0, 1.0]) == [0.5, 3.0]
+
+
+@pytest.mark.parametrize("finished", [True, False])
+def test_large_file_parallel_decode(jne, tmp, finished):
+    """> 65,536 records: the values are decoded by several host threads, from the
+    trailer index (finished) or the scan index (interrupted)."""
+    rng = np.random.default_rng(3)
+    n, k = 300_001, 3
+    seeds = rng.permutation(np.arange(1, 2 * n, 2, dtype=np.uint32))[:n]  # 1- to 3-byte ULEB128 seeds
+    seeds[:3] = [1, 0xFFFFFFFF, 1 << 28]                                   # 1- and 5-byte seeds
+    eigs = rng.standard_normal((n, k))
+    path = os.path.join(tmp, f"big_{finished}.dat")
+    w = jne.DatWriter(path, 1, 2, 64)
+    w.append(seeds, eigs)
+    w.finish() if finished else w.abandon()
+    recs, model, dim, steps = jne.read_dat(path)
+    assert (model, dim, steps) == (1, 2, 64)
+    assert np.array_equal(np.asarray(recs.seeds, dtype=np.uint32), seeds)
+    assert np.array_equal(recs.eigs, eigs)
