@@ -1,4 +1,5 @@
-"""Builds libjne_gb300.so (the C-ABI engine) in-tree for sm_103a.
+"""Builds libjne_gb300.so (the C-ABI engine) in-tree for sm_103a, and the
+command-line driver jne_gb300 linked against it.
 
 Every translation unit under csrc/ is compiled by nvcc in parallel, then linked
 into one shared library next to this file.  Run as a script or call build().
@@ -15,6 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libjne_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "jne_cli.cpp")
+CLI = os.path.join(HERE, "jne_gb300")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
@@ -40,6 +43,8 @@ def _stale(srcs) -> bool:
     deps = srcs + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
     deps.append(os.path.join(HERE, "..", "include", "jne.h"))
     deps.append(os.path.abspath(__file__))
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < os.path.getmtime(CLI_SRC):
+        return True
     return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
 
 
@@ -55,6 +60,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    cxx = os.environ.get("CXX", "g++")
+    res = subprocess.run([cxx, "-O2", "-std=c++17", "-Wall", CLI_SRC, "-o", CLI + ".tmp", "-L" + HERE, "-ljne_gb300",
+                          "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 
