@@ -37,6 +37,12 @@ METRIC = "runs/s at dim12 T=10k, FP64 vs mixed-precision at stated error; p50/p9
 UNIT = "runs/s"
 
 
+# DRAM bytes (read + write) of one k_accum_mixed<12> launch per run, from an ncu
+# capture of the full 200,000-run launch (profiles/k_accum_mixed_dim12_T10k_dram.md):
+# 10,771,200 B read + 417,338,368 B written.  Algorithmic: 2,352 B of record per run.
+ACCUM_DRAM_BYTES_PER_RUN = (10_771_200 + 417_338_368) / 200_000
+
+
 def k_of(model: int) -> int:
     return DIM + 1 if model in (1, 3) else DIM
 
@@ -104,6 +110,23 @@ def measured_peaks():
         return {}
 
 
+def replica_seed_first(rank: int, runs_per_replica: int) -> int:
+    """Replicas (one per GPU) take disjoint, consecutive seed ranges: rank r runs seeds
+    1 + r R .. (r + 1) R, so N replicas cover seeds 1 .. N R exactly once."""
+    return 1 + rank * runs_per_replica
+
+
+def reduce_max(dist, x: float, device: str) -> float:
+    """Max of x over the ranks of the default process group (x itself without one)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_sample(oracle, runs_per_model: int, threads: int, seed_first: int = 1):
     """Oracle (dense restatement) on `threads` host threads; returns runs/s."""
     t0 = time.perf_counter()
@@ -166,7 +189,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     eng = jne.Engine(local, chunk=args.chunk)
     R = args.runs
-    seed0 = 1 + rank * R  # disjoint seed ranges per replica
+    seed0 = replica_seed_first(rank, R)
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
     # requests alternate between two caller streams, so the finalize of one
@@ -185,11 +208,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         torch.cuda.synchronize()
 
     def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(dist, x, "cuda")
 
     # ---- mixed precision, device-resident outputs (value) ----
     for _ in range(args.warmup):
@@ -290,8 +309,11 @@ def run_gpu(args, rank: int, world: int) -> None:
     bf16 = peaks.get("bf16_tflops")
     W = sum(canonical_flops(m) for m in MODELS) / len(MODELS)
     achieved = W * R / (mean_acc_ms * 1e-3) / 1e12
+    traffic = args.traffic if args.traffic is not None else ACCUM_DRAM_BYTES_PER_RUN * R
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-            "frac": (achieved / bf16) if bf16 else None, "traffic": args.traffic,
+            "frac": (achieved / bf16) if bf16 else None, "traffic": traffic,
+            "traffic_note": "ncu dram bytes of one full 200k-run launch, per run x runs per launch; "
+                            "algorithmic bytes are the 2,352 B/run records",
             "kernel": "k_accum_mixed<12,false>", "peak_source": "measured bf16_tflops (burst)" if bf16 else "none",
             "flops_per_run": W}
     normals_rate = DIM * STEPS * R / (mean_acc_ms * 1e-3)
@@ -303,6 +325,18 @@ def run_gpu(args, rank: int, world: int) -> None:
                      "Box-Muller device code alone (jne_probe_rates, measured in this run)"}
 
     ragged = bench_ragged60(jne, torch, local, args.ragged_steps) if args.ragged_steps > 0 and rank == 0 else None
+    precision = bench_precision(jne, torch, local, args.c3_runs) if args.c3_runs > 0 and rank == 0 else None
+    # all five models of the same seeds from one pass over the paths (jne_eigs_seeded_models): the path of a
+    # seed does not depend on the model, so one accumulation serves five finalizes; host outputs
+    eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, min(R, 20_000), precision=jne.PREC_MIXED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, R, precision=jne.PREC_MIXED)
+    one_pass_s = time.perf_counter() - t0
+    one_pass = {"runs_per_s": len(MODELS) * R / one_pass_s, "seconds": one_pass_s,
+                "workload": f"models 0-4 x {R} seeds, dim {DIM}, T {STEPS}, mixed, one accumulation per seed "
+                            "(jne_eigs_seeded_models), eigenvalues copied to host memory; wall clock",
+                "note": "not the headline: the headline runs one request per model, as the reference does"}
     serving = bench_serving(jne, local, args.serve_seconds) if args.serve_seconds > 0 and rank == 0 else None
 
     cpu = None
@@ -338,7 +372,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
             "gpu_launches": acc_n + fin_n,
             "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
-            "ragged60": ragged, "serving": serving,
+            "ragged60": ragged, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
             "cpu_baseline": cpu, "clocks": clk.summary(),
         }))
     eng.close()
@@ -384,6 +418,39 @@ def bench_ragged60(jne, torch, local: int, steps: int) -> dict:
             "replays": steps, "all_finite": finite, "graph": True,
             "workload": "60 (model, dim) pairs, T in {1000,5000,10000} and runs log-uniform [1e4,1e6] per pair "
                         "(seed 0xC4), mixed precision, one persistent ragged launch + ragged finalize per replay"}
+
+
+def bench_precision(jne, torch, local: int, runs: int, subset: int = 10_000) -> dict:
+    """Model 4, dim 12, T 1e4: `runs` runs in mixed precision (device outputs), and the max-eig / trace error
+    of the first `subset` of them against the plain FP64 kernel on the same seeds."""
+    k = jne.eigen_count(4, DIM)
+    out = torch.empty((runs, k), dtype=torch.float64, device="cuda")
+    with jne.Engine(local) as eng:
+        stream = torch.cuda.Stream()
+        eng.eigs_seeded_device(4, DIM, STEPS, 1, min(runs, 100_000), out.data_ptr(), precision=jne.PREC_MIXED,
+                               stream=stream.cuda_stream)  # warm-up
+        eng.sync()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.eigs_seeded_device(4, DIM, STEPS, 1, runs, out.data_ptr(), precision=jne.PREC_MIXED,
+                               stream=stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        eng.sync()
+        ms = a.elapsed_time(b)
+        ns = min(subset, runs)
+        f = eng.eigs_seeded(4, DIM, STEPS, 1, ns, precision=jne.PREC_FP64)
+    x = out[:ns].cpu().numpy()
+    rel_max = np.abs(x[:, 0] - f[:, 0]) / f[:, 0]
+    rel_tr = np.abs(x.sum(1) - f.sum(1)) / f.sum(1)
+    return {"runs": runs, "runs_per_s": runs / (ms * 1e-3), "error_subset": ns,
+            "maxeig_rel_err": {"max": float(rel_max.max()), "p99": float(np.percentile(rel_max, 99)),
+                               "mean": float(rel_max.mean())},
+            "trace_rel_err": {"max": float(rel_tr.max()), "p99": float(np.percentile(rel_tr, 99)),
+                              "mean": float(rel_tr.mean())},
+            "workload": f"model 4, dim {DIM}, T {STEPS}, {runs} runs mixed (seeds 1..{runs}); error of the first "
+                        f"{ns} vs the plain FP64 kernel on the same seeds"}
 
 
 def bench_serving(jne, local: int, seconds: float, rate: float = 200.0, seed: int = 0xC5) -> dict:
@@ -439,9 +506,12 @@ def main() -> None:
     ap.add_argument("--cpu-runs", type=int, default=None, help="CPU sample runs per model (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length without --cpu-runs")
     ap.add_argument("--chunk", type=int, default=0, help="steps per FP32 chunk (0: adaptive, 256 at T=10k)")
-    ap.add_argument("--traffic", type=float, default=None, help="ncu dram bytes per accumulation launch")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per accumulation launch (default: the committed capture, scaled by runs)")
     ap.add_argument("--ragged-steps", type=int, default=2, help="timed replays of the ragged 60-pair plan (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="Poisson arrival window of the serving run (0: skip)")
+    ap.add_argument("--c3-runs", type=int, default=10_000_000,
+                    help="model-4 precision run: mixed runs (error on the first 10,000 vs FP64; 0: skip)")
     ap.add_argument("--rng-peak", type=float, default=None,
                     help="Philox+Box-Muller normals/s (default: measured live by jne_probe_rates)")
     args = ap.parse_args()
