@@ -82,6 +82,30 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float t) {
   lo = __fadd_rn(lo, err);
 }
 
+// Float-float arithmetic of the chunk merge (Knuth's two-sum, the FMA two-product;
+// explicit round-to-nearest so no step is fused away).  A value is hi + lo with
+// |lo| <= ulp(hi) / 2 after renormalisation: about 48 significant bits.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi, lo) += p + t, renormalised
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float p, float t) {
+  float s, e;
+  two_sum(hi, p, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, t));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+// (xh + xl)(yh + yl) = p + e to about 2^-46 relative (e not renormalised)
+__device__ __forceinline__ void ff_mul(float xh, float xl, float yh, float yl, float& p, float& e) {
+  p = __fmul_rn(xh, yh);
+  e = __fmaf_rn(xh, yh, -p);
+  e = __fmaf_rn(xh, yl, e);
+  e = __fmaf_rn(xl, yh, e);
+}
+
 // One 32-step tile of one run.  zrow(f) rows of the staging area hold this
 // tile's increments (zero rows for f >= DIM); see the file comment for the
 // lane <-> (row, step) mapping.
@@ -186,11 +210,12 @@ constexpr int kRecMax = JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2 + 6 * JNE_MAX_DIM + 
 struct alignas(16) WarpSmem {
   float zs[16][kZS];      // increments of the current tile: z[feature][step]
   float cm[16][kCS];      // the chunk's local Gram, staged for the merge
-  double wc[16], tz[16];  // walk at the chunk start, chunk increment totals
-  double rec[kRecMax];    // the run's record: FP64 part
-  float rech[kRecMax];    // ... and float-float centred part
+  float wch[16], wcl[16];  // walk at the chunk start (float-float)
+  float tzh[16], tzl[16];  // chunk increment totals (float-float)
+  float rech[kRecMax];     // the run's record, float-float
   float recl[kRecMax];
-  double mm[16], lm[16];  // per feature: chunk mean m, Lc * m
+  float mmh[16], mml[16];  // per feature: chunk mean m of the walk (float-float)
+  float lmh[16], lml[16];  // Lc * m
   float sbf[16], tzfs[16], cub[16], cuub[16], cuz[16], cuuz[16];
   unsigned short mww_pr[JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2];
 };
@@ -207,13 +232,16 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
   const int g = lane >> 2, q = lane & 3;
   float (*zs)[kZS] = sm.zs;
   float (*cm)[kCS] = sm.cm;
-  double* wc = sm.wc;
-  double* tz = sm.tz;
-  double* rec = sm.rec;
+  float* wch = sm.wch;
+  float* wcl = sm.wcl;
+  float* tzh = sm.tzh;
+  float* tzl = sm.tzl;
   float* rech = sm.rech;
   float* recl = sm.recl;
-  double* mm = sm.mm;
-  double* lm = sm.lm;
+  float* mmh = sm.mmh;
+  float* mml = sm.mml;
+  float* lmh = sm.lmh;
+  float* lml = sm.lml;
   float* sbf = sm.sbf;
   float* tzfs = sm.tzfs;
   float* cub = sm.cub;
@@ -247,13 +275,12 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
   const float invTf = 1.0f / (float)T;
   const uint32_t seed = a.seed_first + (uint32_t)run;
   for (int e = lane; e < NREC; e += 32) {
-    rec[e] = 0.0;
     rech[e] = 0.f;
     recl[e] = 0.f;
   }
   if (lane < 16) {
-    wc[lane] = 0.0;
-    tz[lane] = 0.0;
+    wch[lane] = 0.f;
+    wcl[lane] = 0.f;
   }
   __syncwarp();
 
@@ -312,14 +339,16 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
       cm[g + 8][col + 1] = acc[n][3] + accx[n][3];
     }
     if (q == 0) {
-      if (g < d) tz[g] = (double)chiA + (double)cloA;
-      if (g + 8 < d) tz[g + 8] = (double)chiB + (double)cloB;
+      if (g < d) two_sum(chiA, cloA, tzh[g], tzl[g]);
+      if (g + 8 < d) two_sum(chiB, cloB, tzh[g + 8], tzl[g + 8]);
     }
     __syncwarp();
     // ---- merge into the run's record: W = m + beta (m = chunk mean of W, sum beta = 0),
     //      y = ybar + h (u - ubar).  Every moment splits into a "mean" part, a product of
-    //      chunk means (FP64, one FMA per slot), and a centred local part (FP32, small,
-    //      summed across chunks in float-float). ----
+    //      chunk means (float-float), and a centred local part (FP32, small); both are
+    //      summed across chunks in float-float.  No FP64 instruction: on this GPU one warp's
+    //      FP64 instruction holds the FP64 pipe for ~75 cycles, and the merge would be
+    //      bound by it on short chunks. ----
     const jne_chunk_time ct = a.chunk_tab[c0 / L];
     const float Lcf = (float)Lc, invLcf = 1.0f / Lcf;
     const float P1f = 0.5f * Lcf * (Lcf - 1.0f) * invL;
@@ -327,15 +356,25 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
     const float ub = P1f * invLcf;                 // mean of u over the chunk
     const float sig2 = P2f - P1f * ub;             // sum of (u - ubar)^2
     const float qbar = sig2 * invLcf;              // mean of (u - ubar)^2
-    const float hf = (float)L * invTf, ybf = (float)ct.ybar;
+    const float hf = (float)L * invTf, ybf = ct.ybar_hi;
     if (lane < d) {
       const int f = lane;
       const float Sb = cm[d][f], Sub = cm[d + 1][f], Suub = cm[d + 2][f];
       const float Suz = cm[d + 1][16 + f], Suuz = cm[d + 2][16 + f];
-      const double m = wc[f] + (double)Sb * ct.inv_lc;
-      mm[f] = m;
-      lm[f] = ct.lc * m;
-      const float tzf = (float)tz[f];
+      // m = wc + Sb / Lc: the quotient with its exact remainder
+      const float qh = __fmul_rn(Sb, ct.inv_lc);
+      const float ql = __fmul_rn(__fmaf_rn(-qh, ct.lc, Sb), ct.inv_lc);
+      float mh = wch[f], ml = wcl[f];
+      ff_acc(mh, ml, qh, ql);
+      mmh[f] = mh;
+      mml[f] = ml;
+      float ph, pe;
+      ff_mul(mh, ml, ct.lc, 0.f, ph, pe);
+      float lh, ll = 0.f;
+      two_sum(ph, pe, lh, ll);
+      lmh[f] = lh;
+      lml[f] = ll;
+      const float tzf = tzh[f];
       sbf[f] = Sb;
       tzfs[f] = tzf;
       cub[f] = Sub - ub * Sb;                                              // sum (u-ubar) beta
@@ -349,38 +388,46 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
     const float c1y = hf, c2y = 2.0f * ybf * hf, c2yy = hf * hf;  // y and y^2 coefficients
     for (int e = lane; e < NMWW; e += 32) {
       const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
-      rec[e] += lm[p] * mm[r];
-      ff_add(rech[e], recl[e], cm[p][r] - sbf[p] * sbf[r] * invLcf);
+      float ph, pe;
+      ff_mul(lmh[p], lml[p], mmh[r], mml[r], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, cm[p][r] - sbf[p] * sbf[r] * invLcf));
     }
     for (int t = lane; t < NMW; t += 32) {
       const int pp = t / d, r = t - pp * d, e = NMWW + t;
-      const double w64 = pp == 0 ? 1.0 : pp == 1 ? ct.ybar : ct.y2bar;
+      const float wh = pp == 0 ? 1.f : pp == 1 ? ct.ybar_hi : ct.y2bar_hi;
+      const float wl = pp == 0 ? 0.f : pp == 1 ? ct.ybar_lo : ct.y2bar_lo;
       const float a1 = pp == 0 ? 0.f : pp == 1 ? c1y : c2y, a2 = pp == 2 ? c2yy : 0.f;
-      rec[e] += w64 * lm[r];
-      ff_add(rech[e], recl[e], a1 * cub[r] + a2 * cuub[r]);
+      float ph, pe;
+      ff_mul(wh, wl, lmh[r], lml[r], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cub[r] + a2 * cuub[r]));
     }
     for (int t = lane; t < NNZW; t += 32) {
       const int za = t / d, wb = t - za * d, e = NMWW + NMW + t;
-      rec[e] += tz[za] * mm[wb];
-      ff_add(rech[e], recl[e], cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf);
+      float ph, pe;
+      ff_mul(tzh[za], tzl[za], mmh[wb], mml[wb], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf));
     }
     for (int t = lane; t < 2 * d; t += 32) {
       const int pp = t / d, za = t - pp * d, e = NMWW + NMW + NNZW + d + t;
-      const double w64 = pp == 0 ? ct.ybar : ct.y2bar;
+      const float wh = pp == 0 ? ct.ybar_hi : ct.y2bar_hi, wl = pp == 0 ? ct.ybar_lo : ct.y2bar_lo;
       const float a1 = pp == 0 ? c1y : c2y, a2 = pp == 0 ? 0.f : c2yy;
-      rec[e] += w64 * tz[za];
-      ff_add(rech[e], recl[e], a1 * cuz[za] + a2 * cuuz[za]);
+      float ph, pe;
+      ff_mul(wh, wl, tzh[za], tzl[za], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cuz[za] + a2 * cuuz[za]));
     }
     __syncwarp();
-    if (lane < d) wc[lane] += tz[lane];
+    if (lane < d) ff_acc(wch[lane], wcl[lane], tzh[lane], tzl[lane]);
     __syncwarp();
   }
 
-  // ---- write the record (slot order of jne_common.cuh) ----
-  if (lane < d) rec[jne_slot_Nz1(lane, d)] = wc[lane];
+  // ---- write the record (slot order of jne_common.cuh) in FP64 ----
+  if (lane < d) {
+    rech[jne_slot_Nz1(lane, d)] = wch[lane];
+    recl[jne_slot_Nz1(lane, d)] = wcl[lane];
+  }
   __syncwarp();
   const size_t ld = (size_t)a.mom_ld;
-  for (int e = lane; e < NREC; e += 32) a.mom[(size_t)e * ld + run] = rec[e] + ((double)rech[e] + (double)recl[e]);
+  for (int e = lane; e < NREC; e += 32) a.mom[(size_t)e * ld + run] = (double)rech[e] + (double)recl[e];
   __syncwarp();
 }
 

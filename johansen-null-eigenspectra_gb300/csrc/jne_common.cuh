@@ -133,9 +133,11 @@ __host__ __device__ __forceinline__ int jne_slot_Nzyy(int a, int d) { return d *
 __host__ __device__ __forceinline__ int jne_record_slots(int d) { return d * (d + 1) / 2 + 6 * d + d * d; }
 
 // Per-chunk time constants of the mixed kernel: mean of y and of y^2 over the
-// chunk's columns, its step count and the reciprocal.
+// chunk's columns as float-float pairs (hi + lo), its step count and the
+// reciprocal.
 struct jne_chunk_time {
-  double ybar, y2bar, lc, inv_lc;
+  float ybar_hi, ybar_lo, y2bar_hi, y2bar_lo;
+  float lc, inv_lc, pad0, pad1;
 };
 
 // Argument block of one accumulation launch: runs [0, n_runs) of one

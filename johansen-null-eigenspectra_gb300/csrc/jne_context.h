@@ -208,7 +208,9 @@ inline void fill_chunk_table(int steps, int chunk, jne_chunk_time* dst) {
     // columns i = c0 .. c0+lc-1 carry y = (i+1)/T
     const long double s1 = (long double)lc * (2.0L * c0 + lc + 1.0L) / 2.0L;
     const long double s2 = sq((long double)(c0 + lc)) - sq((long double)c0);
-    dst[ch] = {(double)(s1 / (T * lc)), (double)(s2 / (T * T * lc)), (double)lc, 1.0 / (double)lc};
+    const long double yb = s1 / (T * lc), y2b = s2 / (T * T * lc);
+    const float ybh = (float)yb, y2h = (float)y2b;
+    dst[ch] = {ybh, (float)(yb - ybh), y2h, (float)(y2b - y2h), (float)lc, 1.0f / (float)lc, 0.f, 0.f};
   }
 }
 

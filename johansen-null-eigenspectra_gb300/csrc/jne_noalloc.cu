@@ -63,7 +63,9 @@ __global__ void k_fill_chunk_table(jne_chunk_time* tab, int steps, int chunk, in
   const double s1 = lc * (2.0 * c0 + lc + 1.0) / 2.0;  // sum of (i+1) over the chunk's columns
   // sum of (i+1)^2 = sum_{j=c0+1}^{c0+lc} j^2, written without the large-number cancellation
   const double s2 = lc * (c0 * c0 + c0 * (lc + 1.0)) + lc * (lc + 1.0) * (2.0 * lc + 1.0) / 6.0;
-  tab[ch] = {s1 / (T * lc), s2 / (T * T * lc), lc, 1.0 / lc};
+  const double yb = s1 / (T * lc), y2b = s2 / (T * T * lc);
+  const float ybh = (float)yb, y2h = (float)y2b;
+  tab[ch] = {ybh, (float)(yb - (double)ybh), y2h, (float)(y2b - (double)y2h), (float)lc, 1.0f / (float)lc, 0.f, 0.f};
 }
 
 // FP64 moment entries of a (model, dim) pair, built on the device (the same
