@@ -22,7 +22,7 @@
 // so slot k = q (q+4) of MMA s carries tile step 8q + 2s (8q + 2s + 1): every
 // lane owns 8 consecutive steps, which makes the scan along time cheap, and the
 // A fragment registers double as the B fragments of the G x G tiles.
-#include "jne_kernels.h"
+#include "jne_finalize_run.cuh"
 
 namespace {
 
@@ -431,36 +431,80 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
   __syncwarp();
 }
 
-// One request: every warp strides over its runs.
-// The round keys arrive as a kernel parameter (computed on the host): the
-// Philox rounds read them from the parameter bank instead of holding 20
-// registers.
+// Fused finalize.  Runs are counted per batch of 32 consecutive items; the
+// warp that accumulates the last run of a batch finalizes the whole batch, one
+// run per lane, in FP64 -- a pipe the accumulation leaves idle, so the
+// finalize runs in the shadow of the other warps' accumulation instead of in a
+// second kernel after it.  Every batch is full except the very last, and a
+// lane's record reads are contiguous with its neighbours'.  Ordering: the
+// writers fence their record slots before the count, the finalizing warp
+// fences after it and reads the records from L2.  Returns the first item of
+// the batch to finalize, or -1.
+__device__ __forceinline__ long long batch_complete(unsigned int* batch_done, long long item, long long total,
+                                                    int lane) {
+  __threadfence();
+  __syncwarp();
+  unsigned int seen = 0;
+  if (lane == 0) seen = atomicAdd(&batch_done[item >> 5], 1u);
+  seen = __shfl_sync(0xffffffffu, seen, 0);
+  const long long first = item & ~31ll;
+  const long long cnt = total - first < 32 ? total - first : 32;
+  if ((long long)seen != cnt - 1) return -1;
+  __threadfence();
+  return first;
+}
+
+// One request: every warp strides over its runs.  The round keys arrive as a
+// kernel parameter (computed on the host): the Philox rounds read them from
+// the parameter bank instead of holding 20 registers.  With fin.out set, the
+// kernel also finalizes its runs (fin describes the same request).
 template <int DIM, bool EXT>
 __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
-    k_accum_mixed(const __grid_constant__ jne_accum_args a, const __grid_constant__ jne_round_keys rk) {
+    k_accum_mixed(const __grid_constant__ jne_accum_args a, const __grid_constant__ jne_round_keys rk,
+                  const __grid_constant__ jne_finalize_args fin) {
   __shared__ WarpSmem sm_all[kMixWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nwarps = gridDim.x * kMixWarps;
+  const bool fused = fin.out != nullptr && a.batch_done != nullptr;
+  auto finalize_batch = [&](int run) {
+    const long long first = batch_complete(a.batch_done, run, a.n_runs, lane);
+    if (first >= 0 && first + lane < a.n_runs) jne_fin::finalize_run(fin, (int)(first + lane));
+    __syncwarp();
+  };
   if (a.next_run == nullptr) {
-    for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps)
+    for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps) {
       accum_run<DIM, EXT>(a, run, sm_all[wib], rk, lane);
-    return;
-  }
-  // first run by warp index, then the next free one from the counter
-  for (long long run = blockIdx.x * kMixWarps + wib; run < a.n_runs;) {
-    accum_run<DIM, EXT>(a, (int)run, sm_all[wib], rk, lane);
-    unsigned long long item = 0;
-    if (lane == 0) item = atomicAdd(a.next_run, 1ull);
-    run = nwarps + (long long)__shfl_sync(0xffffffffu, item, 0);
+      if (fused) finalize_batch(run);
+    }
+  } else {
+    // first run by warp index, then the next free one from the counter
+    for (long long run = blockIdx.x * kMixWarps + wib; run < a.n_runs;) {
+      accum_run<DIM, EXT>(a, (int)run, sm_all[wib], rk, lane);
+      if (fused) finalize_batch((int)run);
+      unsigned long long item = 0;
+      if (lane == 0) item = atomicAdd(a.next_run, 1ull);
+      run = nwarps + (long long)__shfl_sync(0xffffffffu, item, 0);
+    }
   }
 }
 
 // A ragged batch of requests (any dims, step counts and sizes) in one
 // persistent launch: each warp takes the next run of the flattened batch from
 // a global counter, so long and short requests share the GPU without tails.
+__device__ __forceinline__ int request_of(const jne_ragged_req* __restrict__ reqs, int n_req, long long item) {
+  int lo = 0, hi = n_req - 1;  // request r with reqs[r].first <= item < reqs[r + 1].first
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (reqs[mid].first <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// batch_done (ceil(total / 32) zeroed counts): every item is also finalized
+// in the launch, batches of 32 consecutive items spanning requests as needed.
 __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
     k_accum_mixed_ragged(const jne_ragged_req* __restrict__ reqs, int n_req, long long total,
-                         unsigned long long* __restrict__ counter) {
+                         unsigned long long* __restrict__ counter, unsigned int* __restrict__ batch_done) {
   __shared__ WarpSmem sm_all[kMixWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   for (;;) {
@@ -468,11 +512,7 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
     if (lane == 0) item = atomicAdd(counter, 1ull);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= (unsigned long long)total) break;
-    int lo = 0, hi = n_req - 1;  // request r with reqs[r].first <= item < reqs[r + 1].first
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if ((unsigned long long)reqs[mid].first <= item) lo = mid; else hi = mid - 1;
-    }
+    const int lo = request_of(reqs, n_req, (long long)item);
     const jne_accum_args& a = reqs[lo].acc;
     const int run = (int)(item - (unsigned long long)reqs[lo].first);
     const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
@@ -490,6 +530,14 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
       case 11: accum_run<11, false>(a, run, sm_all[wib], rk, lane); break;
       default: accum_run<12, false>(a, run, sm_all[wib], rk, lane); break;
     }
+    if (batch_done) {
+      const long long first = batch_complete(batch_done, (long long)item, total, lane);
+      if (first >= 0 && first + lane < total) {
+        const int r = request_of(reqs, n_req, first + lane);
+        jne_fin::finalize_run(reqs[r].fin, (int)(first + lane - reqs[r].first));
+      }
+      __syncwarp();
+    }
   }
 }
 
@@ -506,15 +554,15 @@ int resident_grid(K kernel, int threads, size_t shm, int sms, long long n_runs, 
 }
 
 template <int DIM>
-cudaError_t launch_dim(const jne_accum_args& a, int sms, cudaStream_t st) {
+cudaError_t launch_dim(const jne_accum_args& a, const jne_finalize_args& fin, int sms, cudaStream_t st) {
   const int threads = kMixWarps * JNE_WARP;
   const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
   if (a.ext) {
     auto k = k_accum_mixed<DIM, true>;
-    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk);
+    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk, fin);
   } else {
     auto k = k_accum_mixed<DIM, false>;
-    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk);
+    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk, fin);
   }
   return cudaGetLastError();
 }
@@ -522,30 +570,33 @@ cudaError_t launch_dim(const jne_accum_args& a, int sms, cudaStream_t st) {
 }  // namespace
 
 cudaError_t jne_launch_accum_mixed_ragged(const jne_ragged_req* reqs, int n_req, long long total,
-                                         unsigned long long* counter, int sms, cudaStream_t st) {
+                                         unsigned long long* counter, unsigned int* batch_done, int sms,
+                                         cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   const int threads = kMixWarps * JNE_WARP;
   k_accum_mixed_ragged<<<resident_grid(k_accum_mixed_ragged, threads, 0, sms, total, kMixWarps), threads, 0, st>>>(
-      reqs, n_req, total, counter);
+      reqs, n_req, total, counter, batch_done);
   return cudaGetLastError();
 }
 
-cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, int sms, cudaStream_t st) {
+cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, const jne_finalize_args* fin, int sms, cudaStream_t st) {
   if (a.n_runs <= 0) return cudaSuccess;
   if (a.chunk <= 0 || a.chunk % 32 != 0) return cudaErrorInvalidValue;
+  jne_finalize_args f{};  // out == nullptr: accumulation only
+  if (fin) f = *fin;
   switch (a.dim) {
-    case 1: return launch_dim<1>(a, sms, st);
-    case 2: return launch_dim<2>(a, sms, st);
-    case 3: return launch_dim<3>(a, sms, st);
-    case 4: return launch_dim<4>(a, sms, st);
-    case 5: return launch_dim<5>(a, sms, st);
-    case 6: return launch_dim<6>(a, sms, st);
-    case 7: return launch_dim<7>(a, sms, st);
-    case 8: return launch_dim<8>(a, sms, st);
-    case 9: return launch_dim<9>(a, sms, st);
-    case 10: return launch_dim<10>(a, sms, st);
-    case 11: return launch_dim<11>(a, sms, st);
-    case 12: return launch_dim<12>(a, sms, st);
+    case 1: return launch_dim<1>(a, f, sms, st);
+    case 2: return launch_dim<2>(a, f, sms, st);
+    case 3: return launch_dim<3>(a, f, sms, st);
+    case 4: return launch_dim<4>(a, f, sms, st);
+    case 5: return launch_dim<5>(a, f, sms, st);
+    case 6: return launch_dim<6>(a, f, sms, st);
+    case 7: return launch_dim<7>(a, f, sms, st);
+    case 8: return launch_dim<8>(a, f, sms, st);
+    case 9: return launch_dim<9>(a, f, sms, st);
+    case 10: return launch_dim<10>(a, f, sms, st);
+    case 11: return launch_dim<11>(a, f, sms, st);
+    case 12: return launch_dim<12>(a, f, sms, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -68,12 +68,14 @@ void jne_close(jne_context* c) {
   cudaFree(c->d_ctab);
   cudaFree(c->d_status);
   cudaFree(c->d_next_run);
+  cudaFree(c->d_batch);
   cudaFree(c->d_qscratch);
   if (c->ev_in) cudaEventDestroy(c->ev_in);
   for (int i = 0; i < 2; i++) {
     cudaFree(c->d_reqs[i]);
     cudaFree(c->d_rtab[i]);
     cudaFree(c->d_counter[i]);
+    cudaFree(c->d_bdone[i]);
     cudaFreeHost(c->h_reqs[i]);
     cudaFreeHost(c->h_rtab[i]);
     cudaFree(c->d_momb[i]);
@@ -131,10 +133,10 @@ int jne_eigs_from_increments(jne_context* c, int model, int dim, int steps, cons
   if ((rc = clear_status(c, st))) return rc;
   cudaError_t e = cudaMemcpyAsync(c->d_ext, dB, sizeof(double) * n_ext, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "increment upload");
-  if ((rc = accumulate(c, model, dim, steps, 0, 0, 0, n_runs, precision, c->d_ext, c->d_mom, st))) return rc;
+  jne_finalize_args fa = finalize_args(c, model, dim, steps, n_runs, c->d_mom, c->d_out);
   // FP64 walks the increments as given; the mixed kernel walks dB * sqrt(T)
-  const double zscale = kernel_precision(precision, steps) == JNE_PREC_FP64 ? 1.0 : 1.0 / std::sqrt((double)steps);
-  if ((rc = finalize(c, model, dim, steps, n_runs, zscale, c->d_mom, c->d_out, st))) return rc;
+  if (kernel_precision(precision, steps) == JNE_PREC_FP64) fa.zscale = 1.0;
+  if ((rc = accumulate(c, model, dim, steps, 0, 0, 0, n_runs, precision, c->d_ext, c->d_mom, st, &fa))) return rc;
   e = cudaMemcpyAsync(out, c->d_out, sizeof(double) * n_runs * k, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "result download");
   return check_status(c);
@@ -167,13 +169,15 @@ int jne_eigs_seeded_models(jne_context* c, const int* models, int n_models, int 
     const int n = (int)std::min<int64_t>(per, n_runs - done);
     if ((rc = ensure(c, &c->d_mom, &c->mom_cap, (size_t)n * jne_record_slots(dim), "moment buffer"))) return rc;
     if ((rc = ensure(c, &c->d_out, &c->out_cap, (size_t)n * k_total, "output buffer"))) return rc;
+    // one model: the accumulation finalizes its runs itself; several: one finalize per model
+    const jne_finalize_args f0 = finalize_args(c, models[0], dim, steps, n, c->d_mom, c->d_out);
     if ((rc = accumulate(c, acc_model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
-                         c->d_mom, st)))
+                         c->d_mom, st, n_models == 1 ? &f0 : nullptr)))
       return rc;
     size_t off = 0;
     for (int m = 0; m < n_models; m++) {
       const int k = jne_eigen_count(models[m], dim);
-      if ((rc = finalize(c, models[m], dim, steps, n, zscale, c->d_mom, c->d_out + off, st))) return rc;
+      if (n_models > 1 && (rc = finalize(c, models[m], dim, steps, n, c->d_mom, c->d_out + off, st))) return rc;
       cudaError_t e = cudaMemcpyAsync(outs[m] + (size_t)done * k, c->d_out + off, sizeof(double) * n * k,
                                       cudaMemcpyDeviceToHost, st);
       if (e != cudaSuccess) return cuda_fail(c, e, "result download");

@@ -3,8 +3,9 @@
 //
 // A batch mixes (model, dim, steps, seeds, size) freely.  Mixed-precision
 // requests with steps >= JNE_MIXED_MIN_STEPS go through k_accum_mixed_ragged
-// (one launch; warps pull runs of the flattened batch from a global counter) and
-// k_finalize_ragged; the others run through the per-request path.  The batch
+// (one launch; warps pull runs of the flattened batch from a global counter and
+// finalize every completed batch of 32 runs); the others run through the
+// per-request path.  The batch
 // loop of the reference CLI (src/main.rs:85-136: every model of every dim) is
 // one such batch.
 #include <cstring>
@@ -105,6 +106,12 @@ std::vector<std::vector<Piece>> plan_launches(const jne_request* reqs, const std
   return out;
 }
 
+long long total_runs(const std::vector<Piece>& pieces) {
+  long long n = 0;
+  for (const Piece& p : pieces) n += p.n;
+  return n;
+}
+
 size_t chunks_of(jne_context* c, const jne_request* reqs, const std::vector<Piece>& pieces) {
   size_t n = 0;
   for (const Piece& p : pieces) {
@@ -136,9 +143,9 @@ struct jne_plan {
   jne_ragged_req* d_reqs = nullptr;
   jne_chunk_time* d_tab = nullptr;
   unsigned long long* d_counter = nullptr;
+  unsigned int* d_bdone = nullptr;
   unsigned long long bytes = 0;
   cudaEvent_t done = nullptr;
-  cudaEvent_t cap_acc = nullptr, cap_fin = nullptr;  // fork/join inside the captured graph
 };
 
 extern "C" {
@@ -180,6 +187,7 @@ int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* co
         (rc = ensure(c, &c->d_reqs[b], &c->reqs_cap[b], pieces.size(), "request table")) ||
         (rc = ensure(c, &c->d_rtab[b], &c->rtab_cap[b], ntab, "chunk tables")) ||
         (rc = ensure(c, &c->d_counter[b], &c->counter_cap[b], 1, "work counter")) ||
+        (rc = ensure(c, &c->d_bdone[b], &c->bdone_cap[b], ((size_t)total_runs(pieces) + 31) / 32, "batch counts")) ||
         (rc = ensure_pinned(c, &c->h_reqs[b], &c->h_reqs_cap[b], pieces.size())) ||
         (rc = ensure_pinned(c, &c->h_rtab[b], &c->h_rtab_cap[b], ntab)))
       return rc;
@@ -190,22 +198,16 @@ int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* co
                              cudaMemcpyHostToDevice, st)) != cudaSuccess ||
         (e = cudaMemcpyAsync(c->d_rtab[b], c->h_rtab[b], sizeof(jne_chunk_time) * nt, cudaMemcpyHostToDevice, st)) !=
             cudaSuccess ||
-        (e = cudaMemsetAsync(c->d_counter[b], 0, sizeof(unsigned long long), st)) != cudaSuccess)
+        (e = cudaMemsetAsync(c->d_counter[b], 0, sizeof(unsigned long long), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(c->d_bdone[b], 0, sizeof(unsigned int) * ((total + 31) / 32), st)) != cudaSuccess)
       return cuda_fail(c, e, "batch upload");
     {
       ProfScope ps(c, JNE_KERNEL_ACCUM_MIXED, st);
-      e = jne_launch_accum_mixed_ragged(c->d_reqs[b], (int)pieces.size(), total, c->d_counter[b], c->sms, st);
+      e = jne_launch_accum_mixed_ragged(c->d_reqs[b], (int)pieces.size(), total, c->d_counter[b], c->d_bdone[b],
+                                        c->sms, st);
     }
-    if (e != cudaSuccess) return cuda_fail(c, e, "ragged accumulation launch");
-    if ((e = cudaEventRecord(c->ev_acc[b], st)) != cudaSuccess ||
-        (e = cudaStreamWaitEvent(c->fin_stream, c->ev_acc[b], 0)) != cudaSuccess)
-      return cuda_fail(c, e, "stream order");
-    {
-      ProfScope ps(c, JNE_KERNEL_FINALIZE, c->fin_stream);
-      e = jne_launch_finalize_ragged(c->d_reqs[b], (int)pieces.size(), total, c->sms, c->fin_stream);
-    }
-    if (e != cudaSuccess) return cuda_fail(c, e, "ragged finalize launch");
-    if ((e = cudaEventRecord(c->ev_fin[b], c->fin_stream)) != cudaSuccess) return cuda_fail(c, e, "event record");
+    if (e != cudaSuccess) return cuda_fail(c, e, "ragged launch");
+    if ((e = cudaEventRecord(c->ev_fin[b], st)) != cudaSuccess) return cuda_fail(c, e, "event record");
     c->fin_pending[b] = true;
     last = b;
   }
@@ -234,8 +236,10 @@ int jne_plan_create(jne_context* c, const jne_request* reqs, int n_req, double* 
     slots += (size_t)reqs[i].n_runs * jne_record_slots(reqs[i].dim);
   }
   const size_t ntab = chunks_of(c, reqs, pieces);
+  const size_t nbatch = ((size_t)total_runs(pieces) + 31) / 32;
   const unsigned long long bytes = slots * sizeof(double) + pieces.size() * sizeof(jne_ragged_req) +
-                                   ntab * sizeof(jne_chunk_time) + sizeof(unsigned long long);
+                                   ntab * sizeof(jne_chunk_time) + sizeof(unsigned long long) +
+                                   nbatch * sizeof(unsigned int);
   if (c->in_use + bytes > c->budget)
     return fail(c, JNE_ERR_BUDGET, "plan needs " + std::to_string(bytes) + " bytes beyond the budget");
   if ((rc = drain(c))) return rc;
@@ -248,9 +252,8 @@ int jne_plan_create(jne_context* c, const jne_request* reqs, int n_req, double* 
   if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_reqs, pieces.size() * sizeof(jne_ragged_req));
   if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_tab, ntab * sizeof(jne_chunk_time));
   if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_counter, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_bdone, nbatch * sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->cap_acc, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->cap_fin, cudaEventDisableTiming);
   long long total = 0;
   size_t nt = 0;
   if (e == cudaSuccess) {
@@ -258,18 +261,14 @@ int jne_plan_create(jne_context* c, const jne_request* reqs, int n_req, double* 
     e = cudaMemcpy(p->d_reqs, hr.data(), sizeof(jne_ragged_req) * hr.size(), cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess) e = cudaMemcpy(p->d_tab, ht.data(), sizeof(jne_chunk_time) * nt, cudaMemcpyHostToDevice);
-  // capture: counter reset, ragged accumulation, then the ragged finalize on the
-  // second stream, joined back to the origin stream
+  // capture: counter resets, then the ragged launch (accumulation + fused finalize)
   cudaStream_t st = c->stream;
   if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t ce = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned long long), st);
-    if (ce == cudaSuccess) ce = jne_launch_accum_mixed_ragged(p->d_reqs, (int)pieces.size(), total, p->d_counter, c->sms, st);
-    if (ce == cudaSuccess) ce = cudaEventRecord(p->cap_acc, st);
-    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(c->fin_stream, p->cap_acc, 0);
-    if (ce == cudaSuccess) ce = jne_launch_finalize_ragged(p->d_reqs, (int)pieces.size(), total, c->sms, c->fin_stream);
-    if (ce == cudaSuccess) ce = cudaEventRecord(p->cap_fin, c->fin_stream);
-    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(st, p->cap_fin, 0);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(p->d_bdone, 0, nbatch * sizeof(unsigned int), st);
+    if (ce == cudaSuccess)
+      ce = jne_launch_accum_mixed_ragged(p->d_reqs, (int)pieces.size(), total, p->d_counter, p->d_bdone, c->sms, st);
     e = cudaStreamEndCapture(st, &p->graph);
     if (e == cudaSuccess) e = ce;
   }
@@ -305,12 +304,11 @@ void jne_plan_destroy(jne_plan* p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->done) cudaEventDestroy(p->done);
-  if (p->cap_acc) cudaEventDestroy(p->cap_acc);
-  if (p->cap_fin) cudaEventDestroy(p->cap_fin);
   cudaFree(p->d_mom);
   cudaFree(p->d_reqs);
   cudaFree(p->d_tab);
   cudaFree(p->d_counter);
+  cudaFree(p->d_bdone);
   if (p->exec) c->in_use -= p->bytes;
   delete p;
 }

@@ -154,6 +154,8 @@ struct jne_accum_args {
   unsigned int* status;      // device status word (bit flags), may be null
   unsigned long long* next_run;  // mixed kernel: zeroed work counter for dynamic run
                                  // assignment, or null for a fixed stride per warp
+  unsigned int* batch_done;      // mixed kernel with a fused finalize: zeroed count of
+                                 // accumulated runs per 32-run batch (ceil(n_runs / 32))
 };
 
 // Status bits a kernel may raise (never a trap).

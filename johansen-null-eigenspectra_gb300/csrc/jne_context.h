@@ -33,6 +33,8 @@ struct jne_context {
   size_t ent_cap = 0;
   unsigned int* d_status = nullptr;
   unsigned long long* d_next_run = nullptr;  // work counter of single-request mixed launches
+  unsigned int* d_batch = nullptr;           // per-32-run completion counts of fused finalizes
+  size_t batch_cap = 0;
   unsigned long long* d_qscratch = nullptr;  // percentile analyzer: keys, ranks, histograms
   size_t qscratch_cap = 0;
   std::string err;
@@ -52,6 +54,8 @@ struct jne_context {
   size_t rtab_cap[2] = {0, 0};
   unsigned long long* d_counter[2] = {nullptr, nullptr};
   size_t counter_cap[2] = {0, 0};
+  unsigned int* d_bdone[2] = {nullptr, nullptr};
+  size_t bdone_cap[2] = {0, 0};
   jne_ragged_req* h_reqs[2] = {nullptr, nullptr};
   size_t h_reqs_cap[2] = {0, 0};
   jne_chunk_time* h_rtab[2] = {nullptr, nullptr};
@@ -222,9 +226,32 @@ inline int kernel_precision(int precision, int steps) {
   return (precision == JNE_PREC_MIXED && steps >= JNE_MIXED_MIN_STEPS) ? JNE_PREC_MIXED : JNE_PREC_FP64;
 }
 
-// Moments of runs [seed_first, seed_first + n) into c->d_mom (leading dim n).
+inline int finalize(jne_context* c, const jne_finalize_args& f, cudaStream_t st);
+
+// The finalize argument block of n runs of one request (records in mom).
+inline jne_finalize_args finalize_args(jne_context* c, int model, int dim, int steps, int n, const double* mom,
+                                       double* d_out) {
+  jne_finalize_args f{};
+  f.model = model;
+  f.dim = dim;
+  f.steps = steps;
+  f.n_runs = n;
+  f.zscale = 1.0 / std::sqrt((double)steps);
+  f.ts = time_sums(steps);
+  f.mom = mom;
+  f.mom_ld = n;
+  f.out = d_out;
+  f.status = c->d_status;
+  return f;
+}
+
+// Moments of runs [seed_first, seed_first + n) into mom (leading dim n).  With
+// `fin`, the runs' eigenvalues are also produced on st: inside the mixed
+// kernel (each warp finalizes its runs), or by a finalize launch after the
+// FP64 kernel.
 inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uint32_t key1, uint32_t seed_first,
-               int n, int precision, const double* d_ext, double* mom, cudaStream_t st) {
+                      int n, int precision, const double* d_ext, double* mom, cudaStream_t st,
+                      const jne_finalize_args* fin = nullptr) {
   precision = kernel_precision(precision, steps);
   jne_accum_args a{};
   a.model = model;
@@ -253,8 +280,12 @@ inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t ke
       c->ent_dim = dim;
     }
     const int nent = c->ent_n;
-    ProfScope ps(c, JNE_KERNEL_ACCUM_FP64, st);
-    e = jne_launch_accum_f64(a, c->d_ent, nent, c->sms, st);
+    {
+      ProfScope ps(c, JNE_KERNEL_ACCUM_FP64, st);
+      e = jne_launch_accum_f64(a, c->d_ent, nent, c->sms, st);
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "accumulation launch");
+    return fin ? finalize(c, *fin, st) : JNE_OK;
   } else {
     // per-chunk time means, exact (integer sums) then rounded once
     const int nch = (steps + a.chunk - 1) / a.chunk;
@@ -274,30 +305,31 @@ inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t ke
     e = cudaMemsetAsync(c->d_next_run, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_fail(c, e, "work counter reset");
     a.next_run = c->d_next_run;
+    if (fin) {
+      const size_t nb = ((size_t)n + 31) / 32;
+      int rc = ensure(c, &c->d_batch, &c->batch_cap, nb, "batch counts");
+      if (rc) return rc;
+      e = cudaMemsetAsync(c->d_batch, 0, sizeof(unsigned int) * nb, st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "batch count reset");
+      a.batch_done = c->d_batch;
+    }
     ProfScope ps(c, JNE_KERNEL_ACCUM_MIXED, st);
-    e = jne_launch_accum_mixed(a, c->sms, st);
+    e = jne_launch_accum_mixed(a, fin, c->sms, st);
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "accumulation launch");
   return JNE_OK;
 }
 
-inline int finalize(jne_context* c, int model, int dim, int steps, int n, double zscale, const double* mom, double* d_out,
-             cudaStream_t st) {
-  jne_finalize_args f{};
-  f.model = model;
-  f.dim = dim;
-  f.steps = steps;
-  f.n_runs = n;
-  f.zscale = zscale;
-  f.ts = time_sums(steps);
-  f.mom = mom;
-  f.mom_ld = n;
-  f.out = d_out;
-  f.status = c->d_status;
+inline int finalize(jne_context* c, const jne_finalize_args& f, cudaStream_t st) {
   ProfScope ps(c, JNE_KERNEL_FINALIZE, st);
   cudaError_t e = jne_launch_finalize(f, c->sms, st);
   if (e != cudaSuccess) return cuda_fail(c, e, "finalize launch");
   return JNE_OK;
+}
+
+inline int finalize(jne_context* c, int model, int dim, int steps, int n, const double* mom, double* d_out,
+                    cudaStream_t st) {
+  return finalize(c, finalize_args(c, model, dim, steps, n, mom, d_out), st);
 }
 
 inline int check_common(jne_context* c, int model, int dim, int steps, int64_t n_runs, int precision) {
@@ -340,10 +372,11 @@ inline int join_out(jne_context* c, cudaStream_t user, int last) {
   return e == cudaSuccess ? JNE_OK : cuda_fail(c, e, "stream join");
 }
 
-// Asynchronous seeded batch of one request on the context's two streams: batch
-// b accumulates into record buffer b % 2 on c->stream while the finalize of the
-// previous batch runs on c->fin_stream; events order the buffer reuse.  *last
-// receives the record buffer of the final batch.
+// Asynchronous seeded batch of one request.  Batch b uses record buffer b % 2.
+// Mixed precision: the accumulation kernel finalizes its own runs, on
+// c->stream.  FP64: the finalize of a batch runs on c->fin_stream beside the
+// next batch's accumulation.  Events order the buffer reuse; *last receives
+// the record buffer of the final batch (its ev_fin marks the results).
 inline int enqueue_seeded(jne_context* c, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
                           int64_t n_runs, int precision, double* out_device, int* last) {
   const int k = jne_eigen_count(model, dim);
@@ -351,7 +384,7 @@ inline int enqueue_seeded(jne_context* c, int model, int dim, int steps, uint64_
   stream_key(base_seed, dim, &k0, &k1);
   const int64_t per = batch_runs(c, dim, 0) / 2;  // two record buffers in flight
   if (per < 1) return fail(c, JNE_ERR_BUDGET, "budget too small for one run");
-  const double zscale = 1.0 / std::sqrt((double)steps);
+  const bool fused = kernel_precision(precision, steps) == JNE_PREC_MIXED;
   cudaStream_t st = c->stream;
   cudaError_t e = cudaSuccess;
   int rc;
@@ -362,15 +395,22 @@ inline int enqueue_seeded(jne_context* c, int model, int dim, int steps, uint64_
       return cuda_fail(c, e, "stream wait");
     if ((rc = ensure(c, &c->d_momb[b], &c->momb_cap[b], (size_t)n * jne_record_slots(dim), "moment buffer")))
       return rc;
-    if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
-                         c->d_momb[b], st)))
-      return rc;
-    if ((e = cudaEventRecord(c->ev_acc[b], st)) != cudaSuccess ||
-        (e = cudaStreamWaitEvent(c->fin_stream, c->ev_acc[b], 0)) != cudaSuccess)
-      return cuda_fail(c, e, "stream order");
-    if ((rc = finalize(c, model, dim, steps, n, zscale, c->d_momb[b], out_device + (size_t)done * k, c->fin_stream)))
-      return rc;
-    if ((e = cudaEventRecord(c->ev_fin[b], c->fin_stream)) != cudaSuccess) return cuda_fail(c, e, "event record");
+    const jne_finalize_args fa = finalize_args(c, model, dim, steps, n, c->d_momb[b], out_device + (size_t)done * k);
+    if (fused) {
+      if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
+                           c->d_momb[b], st, &fa)))
+        return rc;
+      if ((e = cudaEventRecord(c->ev_fin[b], st)) != cudaSuccess) return cuda_fail(c, e, "event record");
+    } else {
+      if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
+                           c->d_momb[b], st)))
+        return rc;
+      if ((e = cudaEventRecord(c->ev_acc[b], st)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(c->fin_stream, c->ev_acc[b], 0)) != cudaSuccess)
+        return cuda_fail(c, e, "stream order");
+      if ((rc = finalize(c, fa, c->fin_stream))) return rc;
+      if ((e = cudaEventRecord(c->ev_fin[b], c->fin_stream)) != cudaSuccess) return cuda_fail(c, e, "event record");
+    }
     c->fin_pending[b] = true;
     *last = b;
   }

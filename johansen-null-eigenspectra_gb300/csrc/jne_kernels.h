@@ -28,13 +28,15 @@ struct jne_ragged_req {
   long long first;
 };
 
+// batch_done (may be null): ceil(total / 32) zeroed counts; the launch then
+// also finalizes every item
 cudaError_t jne_launch_accum_mixed_ragged(const jne_ragged_req* reqs, int n_req, long long total,
-                                         unsigned long long* counter, int sms, cudaStream_t st);
-cudaError_t jne_launch_finalize_ragged(const jne_ragged_req* reqs, int n_req, long long total, int sms,
-                                       cudaStream_t st);
+                                         unsigned long long* counter, unsigned int* batch_done, int sms,
+                                         cudaStream_t st);
 cudaError_t jne_launch_accum_f64(const jne_accum_args& a, const int4* ent, int nent, int sms, cudaStream_t st);
 int jne_build_f64_entries(int model, int d, int4* out, int cap);
-cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, int sms, cudaStream_t st);
+// fin (may be null) finalizes the same request's runs inside the launch
+cudaError_t jne_launch_accum_mixed(const jne_accum_args& a, const jne_finalize_args* fin, int sms, cudaStream_t st);
 cudaError_t jne_launch_finalize(const jne_finalize_args& f, int sms, cudaStream_t st);
 cudaError_t jne_launch_export(int dim, int steps, int n_runs, uint32_t seed_first, uint32_t key0, uint32_t key1,
                               double scale, double* out, uint32_t* words, cudaStream_t st);

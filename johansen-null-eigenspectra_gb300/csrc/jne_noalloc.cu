@@ -168,7 +168,7 @@ extern "C" int jne_eigs_seeded_noalloc(int device, int model, int dim, int steps
     if (mixed) {
       k_fill_chunk_table<<<(nch + 127) / 128, 128, 0, st>>>(ctab, steps, chunk, nch);
       e = cudaGetLastError();
-      if (e == cudaSuccess) e = jne_launch_accum_mixed(a, sms, st);
+      if (e == cudaSuccess) e = jne_launch_accum_mixed(a, nullptr, sms, st);
     } else {
       k_fill_entries<<<1, 1, 0, st>>>(ent, model, dim, ent_count);
       e = cudaGetLastError();
