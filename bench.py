@@ -37,10 +37,11 @@ METRIC = "runs/s at dim12 T=10k, FP64 vs mixed-precision at stated error; p50/p9
 UNIT = "runs/s"
 
 
-# DRAM bytes (read + write) of one k_accum_mixed<12> launch per run, from an ncu
-# capture of the full 200,000-run launch (profiles/k_accum_mixed_dim12_T10k_dram.md):
-# 10,771,200 B read + 417,338,368 B written.  Algorithmic: 2,352 B of record per run.
-ACCUM_DRAM_BYTES_PER_RUN = (10_771_200 + 417_338_368) / 200_000
+# DRAM bytes (read + write) of one k_accum_mixed<12> launch (accumulation + fused
+# finalize) per run, from an ncu capture of the full 200,000-run launch
+# (profiles/k_accum_mixed_dim12_T10k_dram.md): 32,402,176 B read + 985,069,312 B written.
+# Algorithmic: 2,352 B of record written and read back, 96 B of eigenvalues per run.
+ACCUM_DRAM_BYTES_PER_RUN = (32_402_176 + 985_069_312) / 200_000
 
 
 def k_of(model: int) -> int:
@@ -312,8 +313,8 @@ def run_gpu(args, rank: int, world: int) -> None:
     traffic = args.traffic if args.traffic is not None else ACCUM_DRAM_BYTES_PER_RUN * R
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
             "frac": (achieved / bf16) if bf16 else None, "traffic": traffic,
-            "traffic_note": "ncu dram bytes of one full 200k-run launch, per run x runs per launch; "
-                            "algorithmic bytes are the 2,352 B/run records",
+            "traffic_note": "ncu dram bytes of one full 200k-run launch (accumulation + fused finalize), per "
+                            "run x runs per launch; algorithmic: 2,352 B/run of records, 96 B/run of eigenvalues",
             "kernel": "k_accum_mixed<12,false>", "peak_source": "measured bf16_tflops (burst)" if bf16 else "none",
             "flops_per_run": W}
     normals_rate = DIM * STEPS * R / (mean_acc_ms * 1e-3)
