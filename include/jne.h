@@ -255,6 +255,14 @@ int jne_simulation_filename(const char* data_dir, int model, int dim, int steps,
 int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int dim, int steps, int64_t num_runs,
                        int precision, uint64_t base_seed, int quiet);
 
+/* The same for several models of one (dim, steps) -- the reference CLI's loop
+ * over models (src/main.rs:109-114).  Models whose files miss the same seeds
+ * (every fresh run) share one pass over the paths: one accumulation per seed,
+ * one finalize per model; each file gets exactly the records and bytes the
+ * per-model driver writes. */
+int jne_simulation_run_models(jne_context* ctx, const char* data_dir, const int* models, int n_models, int dim,
+                              int steps, int64_t num_runs, int precision, uint64_t base_seed, int quiet);
+
 /* Percentiles (simulation_analyzers.rs:4-81) of the trace (stat 0) or the
  * largest eigenvalue (stat 1) of n records of k eigenvalues: linear
  * interpolation at rank p * (n - 1) of the sorted statistic; NaN when n == 0.

@@ -32,7 +32,8 @@ EXPORTS = (
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
     "jne_export_increments", "jne_profile", "jne_profile_read", "jne_probe_rates", "jne_sync",
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
-    "jne_simulation_filename", "jne_simulation_run", "jne_percentiles", "jne_percentiles_device",
+    "jne_simulation_filename", "jne_simulation_run", "jne_simulation_run_models", "jne_percentiles",
+    "jne_percentiles_device",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
     "jne_run_batch", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
     "jne_server_open", "jne_server_submit", "jne_server_wait", "jne_server_fetch", "jne_server_close",
@@ -175,6 +176,8 @@ def lib() -> ctypes.CDLL:
         L.jne_dat_last_error.restype = ctypes.c_char_p
         L.jne_simulation_filename.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, ctypes.c_char_p, ctypes.c_size_t]
         L.jne_simulation_run.argtypes = [vp, ctypes.c_char_p, c_int, c_int, c_int, c_i64, c_int, c_u64, c_int]
+        L.jne_simulation_run_models.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(c_int), c_int, c_int, c_int, c_i64,
+                                                c_int, c_u64, c_int]
         L.jne_percentiles.argtypes = [dp, c_i64, c_int, c_int, dp, c_int, dp]
         _lib = L
     return _lib
@@ -477,6 +480,19 @@ def percentiles(eigs: np.ndarray, stat: str, ps: Sequence[float]) -> List[float]
     _dat_check(lib().jne_percentiles(_dp(e), len(e), e.shape[1], 0 if stat == "trace" else 1, _dp(p), len(p),
                                      _dp(out)))
     return out.tolist()
+
+
+def run_simulations(models: Sequence[int], dim: int, steps: int, num_runs: int, data_dir: str = "data",
+                    precision: int = PREC_MIXED, base_seed: int = DEFAULT_BASE_SEED, quiet: bool = True,
+                    engine: Optional["Engine"] = None) -> None:
+    """run_simulation for several models of one (dim, steps) at once: the same files as one
+    EigenvalueSimulation per model, from one pass over the paths when their missing seeds agree."""
+    eng = engine or default_engine()
+    arr = (ctypes.c_int * len(models))(*[int(m) for m in models])
+    rc = lib().jne_simulation_run_models(eng._h, os.fsencode(data_dir), arr, len(models), dim, steps, num_runs,
+                                         precision, base_seed, int(quiet))
+    if rc != JNE_OK:
+        raise DatError(rc, lib().jne_dat_last_error().decode(errors="replace"))
 
 
 _engine: Optional[Engine] = None

@@ -1,7 +1,8 @@
 // jne_cli.cpp -- command-line driver with the reference's flags (cli.rs:56-132,
-// main.rs:44-136): for every dim in [--dim-start, --dim-end] and every model of
-// --model, run the resumable simulation into data/eigenvalues_model*_dim*_steps*.dat
-// and, unless --quiet, print the trace and max-eigenvalue percentile tables.
+// main.rs:44-136): for every dim in [--dim-start, --dim-end] run the resumable
+// simulation of every model of --model into data/eigenvalues_model*_dim*_steps*.dat
+// (all models of a dim from one pass over the paths) and, unless --quiet, print
+// the trace and max-eigenvalue percentile tables.
 // The runs go to the GPU through the C ABI of libjne_gb300.so; --threads is
 // accepted and validated as in the reference (it sized the CPU thread pool
 // there and has no effect here).  Extra flags: --precision fp64|mixed,
@@ -76,7 +77,9 @@ bool parse_models(const char* s, std::vector<int>* out) {
           std::fprintf(stderr, "Error: invalid model number: %s\n", t.c_str());
           return false;
         }
-        out->push_back((int)v);
+        bool seen = false;  // a repeated model would only find its file complete
+        for (int m : *out) seen = seen || m == (int)v;
+        if (!seen) out->push_back((int)v);
       }
       part.clear();
       if (!*p) break;
@@ -247,13 +250,14 @@ int main(int argc, char** argv) {
     if (!cfg.quiet)
       std::printf("Simulation config: %lld dimensions, %s steps, %s runs\n", dim, with_commas(cfg.steps).c_str(),
                   with_commas(cfg.runs).c_str());
+    // every model of this dim from one pass over the paths (the path of a seed does not depend on the model)
+    rc = jne_simulation_run_models(ctx, cfg.data_dir.c_str(), cfg.models.data(), (int)cfg.models.size(), (int)dim,
+                                   (int)cfg.steps, cfg.runs, cfg.precision, JNE_DEFAULT_BASE_SEED, cfg.quiet ? 1 : 0);
+    if (rc) {
+      std::fprintf(stderr, "Error: dim %lld: %s\n", dim, jne_dat_last_error());
+      break;
+    }
     for (int model : cfg.models) {
-      rc = jne_simulation_run(ctx, cfg.data_dir.c_str(), model, (int)dim, (int)cfg.steps, cfg.runs, cfg.precision,
-                              JNE_DEFAULT_BASE_SEED, cfg.quiet ? 1 : 0);
-      if (rc) {
-        std::fprintf(stderr, "Error: model %d dim %lld: %s\n", model, dim, jne_dat_last_error());
-        break;
-      }
       if (!cfg.quiet && report(cfg, model, (int)dim)) {
         std::fprintf(stderr, "Error: reading results: %s\n", jne_dat_last_error());
         rc = 1;

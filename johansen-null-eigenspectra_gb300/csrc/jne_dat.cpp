@@ -379,65 +379,141 @@ int jne_simulation_filename(const char* data_dir, int model, int dim, int steps,
   return JNE_OK;
 }
 
-int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int dim, int steps, int64_t num_runs,
-                       int precision, uint64_t base_seed, int quiet) {
-  if (!ctx) return dat_fail(JNE_ERR_ARG, "null context");
-  if (jne_eigen_count(model, dim) < 0 || dim > JNE_MAX_DIM || steps < 1 || num_runs < 0 || num_runs > 0xFFFFFFFFll)
-    return dat_fail(JNE_ERR_ARG, "bad simulation parameters");
-  const std::string dir = data_dir && *data_dir ? data_dir : "data";
-  int rc = mkdirs(dir);
-  if (rc) return rc;
-  char path[4096];
-  if ((rc = jne_simulation_filename(dir.c_str(), model, dim, steps, path, sizeof path))) return rc;
+}  // extern "C"
 
-  // progress (progress.rs:11-53): seeds already in the file; other parameters -> start over
+namespace {
+
+// The seeds 1..=num_runs still missing from a model's file (progress.rs:11-61);
+// a file with other parameters is removed (it will be recreated).
+int remaining_seeds(const std::string& dir, int model, int dim, int steps, int64_t num_runs, int quiet,
+                    std::string* path, std::vector<uint32_t>* remaining) {
+  char buf[4096];
+  int rc = jne_simulation_filename(dir.c_str(), model, dim, steps, buf, sizeof buf);
+  if (rc) return rc;
+  *path = buf;
   std::unordered_set<uint32_t> done;
-  if (file_exists(path)) {
+  if (file_exists(buf)) {
     std::vector<unsigned char> b;
     Parsed p;
-    if (read_file(path, &b) == JNE_OK && parse(b, &p) == JNE_OK) {
+    if (read_file(buf, &b) == JNE_OK && parse(b, &p) == JNE_OK) {
       if (p.model != model || p.dim != dim || p.steps != (uint32_t)steps) {
-        if (!quiet) std::printf("WARNING: Existing file has incompatible parameters; recreating %s\n", path);
-        std::remove(path);
+        if (!quiet) std::printf("WARNING: Existing file has incompatible parameters; recreating %s\n", buf);
+        std::remove(buf);
       } else {
         done.insert(p.seeds.begin(), p.seeds.end());
       }
     }
   }
-  std::vector<uint32_t> remaining;  // progress.rs:56-61, seeds 1..=num_runs
+  remaining->clear();
   for (int64_t s = 1; s <= num_runs; s++)
-    if (!done.count((uint32_t)s)) remaining.push_back((uint32_t)s);
-  if (remaining.empty()) {
-    if (!quiet) std::printf("SUCCESS: calculation for this model already completed, skipping\n");
-    return JNE_OK;
+    if (!done.count((uint32_t)s)) remaining->push_back((uint32_t)s);
+  if (!quiet) {
+    if (remaining->empty())
+      std::printf("SUCCESS: calculation for this model already completed, skipping\n");
+    else
+      std::printf("Remaining %zu calculations to complete (model %d, dim %d, steps %d)\n", remaining->size(), model,
+                  dim, steps);
   }
-  if (!quiet)
-    std::printf("Remaining %zu calculations to complete (model %d, dim %d, steps %d)\n", remaining.size(), model,
-                dim, steps);
-  jne_dat_writer* w = nullptr;
-  if ((rc = jne_dat_open(path, model, dim, (uint32_t)steps, &w, nullptr))) return rc;
-  const int k = jne_eigen_count(model, dim);
+  return JNE_OK;
+}
+
+// Runs `remaining` for every model of `models` (all models share the list):
+// one pass over the paths per contiguous seed range (jne_eigs_seeded_models),
+// the records appended to each model's file in seed order.
+int run_models(jne_context* ctx, const std::vector<int>& models, const std::vector<std::string>& paths, int dim,
+               int steps, const std::vector<uint32_t>& remaining, int precision, uint64_t base_seed) {
+  const size_t nm = models.size();
+  std::vector<jne_dat_writer*> w(nm, nullptr);
+  auto abandon = [&]() {
+    for (jne_dat_writer* x : w)
+      if (x) jne_dat_abandon(x);  // keep what was written; a rerun resumes
+  };
+  int rc;
+  for (size_t m = 0; m < nm; m++)
+    if ((rc = jne_dat_open(paths[m].c_str(), models[m], dim, (uint32_t)steps, &w[m], nullptr))) {
+      abandon();
+      return rc;
+    }
   const int64_t batch = 1 << 18;
-  std::vector<double> eig;
+  std::vector<std::vector<double>> eig(nm);
+  std::vector<double*> outs(nm);
   for (size_t i = 0; i < remaining.size();) {
     // largest contiguous seed range starting at remaining[i], capped at `batch`
     size_t j = i + 1;
     while (j < remaining.size() && remaining[j] == remaining[j - 1] + 1 && (int64_t)(j - i) < batch) j++;
     const int64_t n = (int64_t)(j - i);
-    eig.resize((size_t)n * k);
-    rc = jne_eigs_seeded(ctx, model, dim, steps, base_seed, remaining[i], n, precision, eig.data());
+    for (size_t m = 0; m < nm; m++) {
+      eig[m].resize((size_t)n * jne_eigen_count(models[m], dim));
+      outs[m] = eig[m].data();
+    }
+    rc = jne_eigs_seeded_models(ctx, models.data(), (int)nm, dim, steps, base_seed, remaining[i], n, precision,
+                                outs.data());
     if (rc) {
       g_err = jne_last_error(ctx);
-      jne_dat_abandon(w);  // keep what was written; a rerun resumes
+      abandon();
       return rc;
     }
-    if ((rc = jne_dat_append(w, &remaining[i], eig.data(), n, k))) {
-      jne_dat_abandon(w);
-      return rc;
-    }
+    for (size_t m = 0; m < nm; m++)
+      if ((rc = jne_dat_append(w[m], &remaining[i], outs[m], n, jne_eigen_count(models[m], dim)))) {
+        abandon();
+        return rc;
+      }
     i = j;
   }
-  return jne_dat_finish(w);
+  for (size_t m = 0; m < nm; m++) {
+    jne_dat_writer* x = w[m];
+    w[m] = nullptr;
+    if ((rc = jne_dat_finish(x))) {
+      abandon();
+      return rc;
+    }
+  }
+  return JNE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int jne_simulation_run(jne_context* ctx, const char* data_dir, int model, int dim, int steps, int64_t num_runs,
+                       int precision, uint64_t base_seed, int quiet) {
+  return jne_simulation_run_models(ctx, data_dir, &model, 1, dim, steps, num_runs, precision, base_seed, quiet);
+}
+
+int jne_simulation_run_models(jne_context* ctx, const char* data_dir, const int* models, int n_models, int dim,
+                              int steps, int64_t num_runs, int precision, uint64_t base_seed, int quiet) {
+  if (!ctx) return dat_fail(JNE_ERR_ARG, "null context");
+  if (!models || n_models < 1 || n_models > 5) return dat_fail(JNE_ERR_ARG, "1..5 models required");
+  for (int m = 0; m < n_models; m++) {
+    if (jne_eigen_count(models[m], dim) < 0 || dim > JNE_MAX_DIM)
+      return dat_fail(JNE_ERR_ARG, "bad simulation parameters");
+    for (int q = 0; q < m; q++)
+      if (models[q] == models[m]) return dat_fail(JNE_ERR_ARG, "a model is listed twice");
+  }
+  if (steps < 1 || num_runs < 0 || num_runs > 0xFFFFFFFFll) return dat_fail(JNE_ERR_ARG, "bad simulation parameters");
+  const std::string dir = data_dir && *data_dir ? data_dir : "data";
+  int rc = mkdirs(dir);
+  if (rc) return rc;
+  // models that still miss seeds, grouped by their missing-seed list: models
+  // with the same list (every fresh run) share one pass over the paths
+  std::vector<std::vector<uint32_t>> rem(n_models);
+  std::vector<std::string> path(n_models);
+  for (int m = 0; m < n_models; m++)
+    if ((rc = remaining_seeds(dir, models[m], dim, steps, num_runs, quiet, &path[m], &rem[m]))) return rc;
+  std::vector<bool> taken(n_models, false);
+  for (int m = 0; m < n_models; m++) {
+    if (taken[m] || rem[m].empty()) continue;
+    std::vector<int> group;
+    std::vector<std::string> gpath;
+    for (int q = m; q < n_models; q++)
+      if (!taken[q] && rem[q] == rem[m]) {
+        taken[q] = true;
+        group.push_back(models[q]);
+        gpath.push_back(path[q]);
+      }
+    if ((rc = run_models(ctx, group, gpath, dim, steps, rem[m], precision, base_seed))) return rc;
+  }
+  return JNE_OK;
 }
 
 int jne_percentiles(const double* eigs, int64_t n, int k, int stat, const double* ps, int np, double* out) {

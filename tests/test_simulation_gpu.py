@@ -120,3 +120,29 @@ def test_percentiles_from_simulation(jne, engine, data_dir):  # examples/library
     assert s.calculate_trace_percentiles(p) == jne.percentiles(d.eigs, "trace", p)
     mx = s.calculate_maxeig_percentiles(p)
     assert mx == sorted(mx) and mx[0] > 0
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_all_models_in_one_pass_write_the_same_files(jne, engine, tmp_path, prec):
+    """jne_simulation_run_models: one pass over the paths for every model, files byte-identical
+    to one EigenvalueSimulation per model."""
+    one, many = str(tmp_path / "one"), str(tmp_path / "many")
+    for m in range(5):
+        sim(jne, engine, m, 3, 600, 777, one, precision=prec).run_simulation_quiet()
+    jne.run_simulations(range(5), 3, 600, 777, data_dir=many, precision=prec, engine=engine)
+    for m in range(5):
+        name = f"eigenvalues_model{m}_dim3_steps600.dat"
+        assert open(os.path.join(one, name), "rb").read() == open(os.path.join(many, name), "rb").read()
+
+
+def test_all_models_resume_from_different_points(jne, engine, data_dir):
+    # model 1 already has 300 runs, model 4 has all 500, models 0 and 2 none
+    sim(jne, engine, 1, 2, 400, 300, data_dir).run_simulation_quiet()
+    sim(jne, engine, 4, 2, 400, 500, data_dir).run_simulation_quiet()
+    jne.run_simulations([0, 1, 2, 4], 2, 400, 500, data_dir=data_dir, engine=engine)
+    for m in (0, 1, 2, 4):
+        d = sim(jne, engine, m, 2, 400, 500, data_dir).read_data().sorted_by_seed()
+        assert list(d.seeds) == list(range(1, 501))
+        assert np.array_equal(d.eigs, engine.eigs_seeded(m, 2, 400, 1, 500, precision=jne.PREC_MIXED))
+    with pytest.raises(jne.DatError):
+        jne.run_simulations([0, 0], 2, 400, 10, data_dir=data_dir, engine=engine)
