@@ -158,7 +158,6 @@ int jne_eigs_seeded_models(jne_context* c, const int* models, int n_models, int 
   stream_key(base_seed, dim, &k0, &k1);
   // a single FP64 pass needs every moment any requested model uses
   const int acc_model = (n_models == 1) ? models[0] : -1;
-  const double zscale = 1.0 / std::sqrt((double)steps);
   cudaStream_t st = c->stream;
   int rc = drain(c);
   if (rc) return rc;
@@ -169,7 +168,9 @@ int jne_eigs_seeded_models(jne_context* c, const int* models, int n_models, int 
     const int n = (int)std::min<int64_t>(per, n_runs - done);
     if ((rc = ensure(c, &c->d_mom, &c->mom_cap, (size_t)n * jne_record_slots(dim), "moment buffer"))) return rc;
     if ((rc = ensure(c, &c->d_out, &c->out_cap, (size_t)n * k_total, "output buffer"))) return rc;
-    // one model: the accumulation finalizes its runs itself; several: one finalize per model
+    // one model: the accumulation finalizes its runs itself; several: one finalize kernel per model
+    // (finalizing five models per batch inside the accumulation stalls its warps longer than the
+    // separate kernels take: 0.14 s against 0.08 s for 5 x 200k runs)
     const jne_finalize_args f0 = finalize_args(c, models[0], dim, steps, n, c->d_mom, c->d_out);
     if ((rc = accumulate(c, acc_model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
                          c->d_mom, st, n_models == 1 ? &f0 : nullptr)))
