@@ -324,6 +324,13 @@ def run_gpu(args, rank: int, world: int) -> None:
              "frac": normals_rate / rng_peak, "probe_rates": rates,
              "note": "normals/s the accumulation kernel draws vs the rate of the same Philox4x32-10 + "
                      "Box-Muller device code alone (jne_probe_rates, measured in this run)"}
+    # the tensor work the kernel executes: per 8 steps, 3 Gram blocks x 3 split products of m16n8k8 TF32
+    # (2,048 flops each); against mma.sync TF32 measured by the probe in this run
+    mma_flops = 9 * 2048 * (STEPS // 8) * R / (mean_acc_ms * 1e-3)
+    roof["tensor_pipe"] = {"executed_tflops": mma_flops / 1e12, "peak_tflops": rates["mma_tf32_flops"] / 1e12,
+                           "frac": mma_flops / rates["mma_tf32_flops"],
+                           "note": "executed split-TF32 mma.sync work (not algorithmic flops) vs the measured "
+                                   "mma.sync TF32 rate"}
 
     ragged = bench_ragged60(jne, torch, local, args.ragged_steps) if args.ragged_steps > 0 and rank == 0 else None
     precision = bench_precision(jne, torch, local, args.c3_runs) if args.c3_runs > 0 and rank == 0 else None
