@@ -333,6 +333,8 @@ def run_gpu(args, rank: int, world: int) -> None:
                                    "mma.sync TF32 rate"}
 
     ragged = bench_ragged60(jne, torch, local, args.ragged_steps) if args.ragged_steps > 0 and rank == 0 else None
+    ragged_tuned = (bench_ragged60(jne, torch, local, args.ragged_steps, tune=args.tune_err)
+                    if args.ragged_steps > 0 and args.tune_err > 0 and rank == 0 else None)
     precision = bench_precision(jne, torch, local, args.c3_runs) if args.c3_runs > 0 and rank == 0 else None
     # all five models of the same seeds from one pass over the paths (jne_eigs_seeded_models): the path of a
     # seed does not depend on the model, so one accumulation serves five finalizes; host outputs
@@ -380,7 +382,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
             "gpu_launches": acc_n + fin_n,
             "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
-            "ragged60": ragged, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
+            "ragged60": ragged, "ragged60_tuned": ragged_tuned, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
             "cpu_baseline": cpu, "clocks": clk.summary(),
         }))
     eng.close()
@@ -399,13 +401,26 @@ def ragged60_requests(seed: int = 0xC4):
     return reqs
 
 
-def bench_ragged60(jne, torch, local: int, steps: int) -> dict:
-    """One persistent launch over the ragged 60-pair batch, captured as a CUDA graph and replayed."""
+def tune_classes(eng, classes, max_rel_err: float) -> dict:
+    """Chunk autotuner over the (dim, steps) classes of a workload; returns {"dim x 2^b": chunk}."""
+    out = {}
+    for dim, steps in sorted(set(classes)):
+        if steps >= 256:
+            chunk, _ = eng.autotune_chunk(dim, steps, max_rel_err=max_rel_err, sample_runs=256)
+            out[f"{dim}x{1 << (steps.bit_length() - 1)}"] = chunk
+    eng.set_chunk(-1)  # CHUNK_TUNED
+    return out
+
+
+def bench_ragged60(jne, torch, local: int, steps: int, tune: float = 0.0) -> dict:
+    """One persistent launch over the ragged 60-pair batch, captured as a CUDA graph and replayed.
+    With tune > 0 the chunk lengths come from the autotuner at that error bound."""
     reqs = ragged60_requests()
     total = sum(r["n_runs"] for r in reqs)
     outs = [torch.empty((r["n_runs"], jne.eigen_count(r["model"], r["dim"])), dtype=torch.float64, device="cuda")
             for r in reqs]
     with jne.Engine(local) as eng:
+        chunks = tune_classes(eng, [(r["dim"], r["steps"]) for r in reqs], tune) if tune > 0 else None
         plan = eng.plan(reqs, [o.data_ptr() for o in outs])
         stream = torch.cuda.Stream()
         plan.launch(stream.cuda_stream)  # warm-up replay
@@ -424,6 +439,7 @@ def bench_ragged60(jne, torch, local: int, steps: int) -> dict:
     finite = all(bool(torch.isfinite(o).all()) for o in outs)
     return {"runs_per_s": total / (ms * 1e-3), "ms_per_replay": ms, "requests": len(reqs), "total_runs": total,
             "replays": steps, "all_finite": finite, "graph": True,
+            "chunks": f"autotuned at max error {tune:g}: {chunks}" if chunks else "default rule",
             "workload": "60 (model, dim) pairs, T in {1000,5000,10000} and runs log-uniform [1e4,1e6] per pair "
                         "(seed 0xC4), mixed precision, one persistent ragged launch + ragged finalize per replay"}
 
@@ -518,6 +534,8 @@ def main() -> None:
                     help="ncu dram bytes per accumulation launch (default: the committed capture, scaled by runs)")
     ap.add_argument("--ragged-steps", type=int, default=2, help="timed replays of the ragged 60-pair plan (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="Poisson arrival window of the serving run (0: skip)")
+    ap.add_argument("--tune-err", type=float, default=1e-6,
+                    help="error bound of the chunk autotuner for the tuned ragged line (0: skip)")
     ap.add_argument("--c3-runs", type=int, default=10_000_000,
                     help="model-4 precision run: mixed runs (error on the first 10,000 vs FP64; 0: skip)")
     ap.add_argument("--rng-peak", type=float, default=None,

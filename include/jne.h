@@ -72,8 +72,25 @@ void jne_close(jne_context* ctx);
 const char* jne_last_error(const jne_context* ctx);
 
 /* Steps per FP32 chunk of the mixed kernel: a multiple of 32, or 0 (the
- * default) for about steps/32 rounded down to a power of two in [32, 256]. */
+ * default) for about steps/32 rounded down to a power of two in [32, 256], or
+ * JNE_CHUNK_TUNED for the lengths jne_autotune_chunk chose (the default rule
+ * for classes it has not tuned). */
+#define JNE_CHUNK_TUNED (-1)
 int jne_set_chunk(jne_context* ctx, int chunk);
+
+/* Autotuner of the mixed kernel's chunk length, the speed / accuracy knob of
+ * the mixed path: longer chunks mean fewer FP64-exact merges (faster) and more
+ * FP32 accumulation per chunk (less accurate).  For the class of (dim, steps)
+ * -- steps in [2^b, 2^(b+1)), tuned at 2^b where errors are largest -- it runs
+ * seeds 1..sample_runs of all five models with the FP64 kernel and with each
+ * candidate chunk 32, 64, ... (at most 1024 and half the steps), and keeps the
+ * longest chunk up to which every candidate's largest error stays within
+ * max_rel_err: max-eigenvalue and trace differences relative to max(value, 1).
+ * The choice is stored in ctx for JNE_CHUNK_TUNED.  Classes below
+ * JNE_MIXED_MIN_STEPS run the FP64 kernel and are not tuned (JNE_ERR_ARG).
+ * chunk_out / err_out (the chosen chunk's error) may be null. */
+int jne_autotune_chunk(jne_context* ctx, int dim, int steps, double max_rel_err, int sample_runs, int* chunk_out,
+                       double* err_out);
 
 /* Eigenvalues of n_runs runs from explicit increments.  dB holds n_runs
  * consecutive dim x steps column-major matrices (dB[:, i] = B_{i+1} - B_i,

@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(HERE, "libjne_gb300.so")
 
 JNE_OK, JNE_ERR_ARG, JNE_ERR_BUDGET, JNE_ERR_CUDA, JNE_ERR_TIMEOUT, JNE_ERR_NUMERIC, JNE_ERR_IO, JNE_ERR_FORMAT = range(8)
 PREC_FP64, PREC_MIXED = 0, 1
+CHUNK_TUNED = -1
 DEFAULT_BASE_SEED = 0x4A4F48
 MAX_DIM = 12
 
@@ -30,7 +31,7 @@ MAX_DIM = 12
 EXPORTS = (
     "jne_version", "jne_eigen_count", "jne_open", "jne_close", "jne_last_error", "jne_set_chunk",
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
-    "jne_export_increments", "jne_profile", "jne_profile_read", "jne_probe_rates", "jne_sync",
+    "jne_export_increments", "jne_profile", "jne_profile_read", "jne_probe_rates", "jne_sync", "jne_autotune_chunk",
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
     "jne_simulation_filename", "jne_simulation_run", "jne_simulation_run_models", "jne_percentiles",
     "jne_percentiles_device",
@@ -165,6 +166,7 @@ def lib() -> ctypes.CDLL:
         L.jne_profile.argtypes = [vp, c_int]
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
         L.jne_probe_rates.argtypes = [vp, dp]
+        L.jne_autotune_chunk.argtypes = [vp, c_int, c_int, ctypes.c_double, c_int, ctypes.POINTER(c_int), dp]
         L.jne_percentiles_device.argtypes = [vp, vp, c_i64, c_int, c_int, dp, c_int, dp, vp]
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
         L.jne_dat_open.argtypes = [ctypes.c_char_p, c_int, c_int, c_u32, ctypes.POINTER(vp), i64p]
@@ -222,7 +224,16 @@ class Engine:
             raise JneError(rc, self._L.jne_last_error(self._h).decode(errors="replace"))
 
     def set_chunk(self, chunk: int) -> None:
+        """Steps per FP32 chunk of the mixed kernel: 0 (default rule), CHUNK_TUNED or a multiple of 32."""
         self._check(self._L.jne_set_chunk(self._h, chunk))
+
+    def autotune_chunk(self, dim: int, steps: int, max_rel_err: float = 5e-7, sample_runs: int = 512) -> Tuple[int, float]:
+        """The longest chunk whose error vs the FP64 kernel stays within max_rel_err on the sample,
+        for steps in [2^b, 2^(b+1)); used after set_chunk(CHUNK_TUNED).  Returns (chunk, its error)."""
+        ch, err = ctypes.c_int(), np.zeros(1)
+        self._check(self._L.jne_autotune_chunk(self._h, dim, steps, float(max_rel_err), sample_runs, ctypes.byref(ch),
+                                               _dp(err)))
+        return ch.value, float(err[0])
 
     def profile(self, enable: bool = True) -> None:
         """Bracket every kernel launch with CUDA events on its launching stream."""

@@ -91,8 +91,8 @@ const char* jne_last_error(const jne_context* c) { return c ? c->err.c_str() : k
 
 int jne_set_chunk(jne_context* c, int chunk) {
   if (!c) return JNE_ERR_ARG;
-  if (chunk != 0 && (chunk < 32 || chunk % 32 != 0 || chunk > (1 << 20)))
-    return fail(c, JNE_ERR_ARG, "chunk must be 0 (adaptive) or a multiple of 32");
+  if (chunk != 0 && chunk != JNE_CHUNK_TUNED && (chunk < 32 || chunk % 32 != 0 || chunk > (1 << 20)))
+    return fail(c, JNE_ERR_ARG, "chunk must be 0 (adaptive), JNE_CHUNK_TUNED or a multiple of 32");
   c->chunk = chunk;
   return JNE_OK;
 }

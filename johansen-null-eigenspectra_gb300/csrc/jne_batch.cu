@@ -45,7 +45,7 @@ void describe(jne_context* c, const jne_request* reqs, double* const* outs, cons
     const jne_request& r = reqs[p.req];
     jne_ragged_req& d = hr[i];
     std::memset(&d, 0, sizeof d);
-    const int chunk = c->chunk ? c->chunk : adaptive_chunk(r.steps);
+    const int chunk = chunk_for(c, r.dim, r.steps);
     const int nch = (r.steps + chunk - 1) / chunk;
     uint32_t k0, k1;
     stream_key(r.base_seed, r.dim, &k0, &k1);
@@ -115,7 +115,7 @@ long long total_runs(const std::vector<Piece>& pieces) {
 size_t chunks_of(jne_context* c, const jne_request* reqs, const std::vector<Piece>& pieces) {
   size_t n = 0;
   for (const Piece& p : pieces) {
-    const int chunk = c->chunk ? c->chunk : adaptive_chunk(reqs[p.req].steps);
+    const int chunk = chunk_for(c, reqs[p.req].dim, reqs[p.req].steps);
     n += (size_t)((reqs[p.req].steps + chunk - 1) / chunk);
   }
   return n;

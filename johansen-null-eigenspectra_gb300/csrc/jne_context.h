@@ -3,7 +3,9 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/jne.h"
@@ -14,7 +16,8 @@ struct jne_context {
   int sms = 0;
   unsigned long long budget = 0;
   unsigned long long in_use = 0;
-  int chunk = 0;  // 0: chunk length chosen from the step count
+  int chunk = 0;  // 0: chunk length chosen from the step count; JNE_CHUNK_TUNED: tuned table
+  std::map<std::pair<int, int>, int> tuned_chunk;  // (dim, floor(log2 steps)) -> chunk
   jne_chunk_time* d_ctab = nullptr;
   size_t ctab_cap = 0;
   std::vector<jne_chunk_time> h_ctab;
@@ -162,6 +165,22 @@ inline int adaptive_chunk(int steps) {
   return L;
 }
 
+inline int steps_bucket(int steps) {
+  int b = 0;
+  while ((2ll << b) <= steps) b++;
+  return b;  // 2^b <= steps < 2^(b+1)
+}
+
+// The mixed kernel's chunk length for a request of (dim, steps).
+inline int chunk_for(const jne_context* c, int dim, int steps) {
+  if (c->chunk > 0) return c->chunk;
+  if (c->chunk == JNE_CHUNK_TUNED) {
+    const auto it = c->tuned_chunk.find({dim, steps_bucket(steps)});
+    if (it != c->tuned_chunk.end()) return it->second;
+  }
+  return adaptive_chunk(steps);
+}
+
 inline bool valid_model_dim(int model, int dim) { return model >= 0 && model <= 4 && dim >= 1 && dim <= JNE_MAX_DIM; }
 
 inline jne_time_sums time_sums(int steps) {
@@ -261,7 +280,7 @@ inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t ke
   a.seed_first = seed_first;
   a.key0 = key0;
   a.key1 = key1;
-  a.chunk = c->chunk ? c->chunk : adaptive_chunk(steps);
+  a.chunk = chunk_for(c, dim, steps);
   a.ext = d_ext;
   a.ext_inv_scale = std::sqrt((double)steps);
   a.mom = mom;
