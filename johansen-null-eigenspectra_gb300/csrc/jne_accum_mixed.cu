@@ -106,22 +106,38 @@ __device__ __forceinline__ void ff_mul(float xh, float xl, float yh, float yl, f
   e = __fmaf_rn(xl, yh, e);
 }
 
-// One 32-step tile of one run.  zrow(f) rows of the staging area hold this
-// tile's increments (zero rows for f >= DIM); see the file comment for the
-// lane <-> (row, step) mapping.
+// Dims up to 4 pack two runs into a warp: run A owns G rows 0..7, run B rows
+// 8..15 (walk rows 0..DIM-1, basis rows DIM..DIM+2, then zero rows), so lane g
+// holds local row g of both runs.  The three Gram blocks are then run A's G x G,
+// run B's G x G and G x [z of run A | z of run B]: two runs for the tensor work
+// of one, and two runs' increments per producer lane.
+template <int DIM>
+struct Packing {
+  static constexpr bool kPair = DIM <= JNE_PACK_MAX_DIM;
+  static constexpr int kRuns = kPair ? 2 : 1;
+};
+
+// One 32-step tile of one run (or of two, packed).  The staging area holds the
+// tile's increments: row f = feature f (unpacked), or row 8 r + f = feature f of
+// run r (packed); rows without a feature are zero.  See the file comment for
+// the lane <-> (row, step) mapping.
 template <int DIM, bool FULL>
 __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, int tloc, int nvalid,
                                           float invL, const float (&cA)[4], const float (&cB)[4],
                                           float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[3][4],
                                           float (&accx)[3][4]) {
-  // zA: increments of row g; zB: of row 8 + (g & 3) -- the walk of row g + 8
-  // for g < 4, the B operand of Gram block 1 for g >= 4 (rows >= DIM are zero)
+  // Unpacked: zA = increments of row g; zB = of row 8 + (g & 3) -- the walk of
+  // row g + 8 for g < 4, the B operand of Gram block 1 for g >= 4.  Packed:
+  // zA = run A's feature g for g < 4, run B's feature g - 4 for g >= 4 (the B
+  // operand of block 2); zB = run B's feature g & 3 (its walk for g < 4).
+  constexpr bool PAIR = Packing<DIM>::kPair;
   float zA[8], zB[8];
   {
-    const float4 p0 = *reinterpret_cast<const float4*>(&zs[g][8 * q]);
-    const float4 p1 = *reinterpret_cast<const float4*>(&zs[g][8 * q + 4]);
+    const int ra = PAIR ? (g < 4 ? g : g + 4) : g;
+    const float4 p0 = *reinterpret_cast<const float4*>(&zs[ra][8 * q]);
+    const float4 p1 = *reinterpret_cast<const float4*>(&zs[ra][8 * q + 4]);
     zA[0] = p0.x; zA[1] = p0.y; zA[2] = p0.z; zA[3] = p0.w; zA[4] = p1.x; zA[5] = p1.y; zA[6] = p1.z; zA[7] = p1.w;
-    if (DIM > 8) {
+    if (DIM > 8 || PAIR) {
       const float4 r0 = *reinterpret_cast<const float4*>(&zs[8 + (g & 3)][8 * q]);
       const float4 r1 = *reinterpret_cast<const float4*>(&zs[8 + (g & 3)][8 * q + 4]);
       zB[0] = r0.x; zB[1] = r0.y; zB[2] = r0.z; zB[3] = r0.w; zB[4] = r1.x; zB[5] = r1.y; zB[6] = r1.z; zB[7] = r1.w;
@@ -176,26 +192,28 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   ff_add(chiA, cloA, tileA);
   ff_add(chiB, cloB, tileB);
 
-  // Gram blocks (16 G rows x 8 columns each):
+  // Gram blocks (16 G rows x 8 columns each), unpacked:
   //   0: G x walk 0..7;  1 (DIM > 8): G x [walk 8..11 | z 8..11];  2: G x z 0..7.
   // Block 1's column g is walk row 8 + g (held as GB by lane g < 4) or z row
-  // 8 + g - 4 (held as zB by lane g >= 4).  Products of the basis rows with
-  // themselves are known in closed form and never formed.
+  // 8 + g - 4 (held as zB by lane g >= 4).  Packed: 0: G x run A's rows,
+  // 1: G x run B's rows (GB), 2: G x [z of A | z of B] (zA).  Products of the
+  // basis rows with themselves are known in closed form and never formed.
+  constexpr bool BLOCK1 = DIM > 8 || PAIR;
   float BB[8];
 #pragma unroll
-  for (int j = 0; j < 8; j++) BB[j] = g < 4 ? GB[j] : zB[j];
+  for (int j = 0; j < 8; j++) BB[j] = (PAIR || g < 4) ? GB[j] : zB[j];
   float hh[3][4];
-  if (DIM <= 8)
+  if (!BLOCK1)
 #pragma unroll
     for (int r = 0; r < 4; r++) hh[1][r] = 0.f;
   mma_split<true>(hh[0], accx[0], GA[0], GB[0], GA[1], GB[1], GA[0], GA[1]);
-  if (DIM > 8) mma_split<true>(hh[1], accx[1], GA[0], GB[0], GA[1], GB[1], BB[0], BB[1]);
+  if (BLOCK1) mma_split<true>(hh[1], accx[1], GA[0], GB[0], GA[1], GB[1], BB[0], BB[1]);
   mma_split<true>(hh[2], accx[2], GA[0], GB[0], GA[1], GB[1], zA[0], zA[1]);
 #pragma unroll
   for (int s = 1; s < 4; s++) {
     const int j0 = 2 * s, j1 = 2 * s + 1;
     mma_split<false>(hh[0], accx[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
-    if (DIM > 8) mma_split<false>(hh[1], accx[1], GA[j0], GB[j0], GA[j1], GB[j1], BB[j0], BB[j1]);
+    if (BLOCK1) mma_split<false>(hh[1], accx[1], GA[j0], GB[j0], GA[j1], GB[j1], BB[j0], BB[j1]);
     mma_split<false>(hh[2], accx[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
   }
   // empty the tile's hi*hi accumulator into the chunk sum (round to nearest)
@@ -220,16 +238,29 @@ struct alignas(16) WarpSmem {
   unsigned short mww_pr[JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2];
 };
 
-// One run (seed a.seed_first + run) of a request: accumulate its moment record
-// into a.mom[slot * a.mom_ld + run].  Executed by a whole warp.
+// Lanes that own a walk feature in the merge: lane f < DIM, or (packed) lane
+// 8 r + f of run r.
+template <int DIM>
+__device__ __forceinline__ bool lane_feature_of(int lane) {
+  return Packing<DIM>::kPair ? (lane < 16 && (lane & 7) < DIM) : lane < DIM;
+}
+
+// One unit of a request: run `unit`, or (packed dims) runs 2 unit and
+// 2 unit + 1 -- the second only if the request has it: accumulate their moment
+// records into a.mom[slot * a.mom_ld + run].  Executed by a whole warp.
 template <int DIM, bool EXT>
-__device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, WarpSmem& sm, const jne_round_keys& rk,
-                                          int lane) {
+__device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, WarpSmem& sm, const jne_round_keys& rk,
+                                           int lane) {
   constexpr int d = DIM;
+  constexpr bool PAIR = Packing<DIM>::kPair;
+  constexpr int NU = Packing<DIM>::kRuns;
   constexpr int NQ = (d + 3) / 4;
   constexpr int NMWW = d * (d + 1) / 2, NMW = 3 * d, NNZW = d * d;
   constexpr int NREC = NMWW + NMW + NNZW + 3 * d;  // == jne_record_slots(d)
+  static_assert(NU * NREC <= kRecMax, "records of a unit fit the shared record");
   const int g = lane >> 2, q = lane & 3;
+  const int run0 = NU * unit;
+  const int nrun = min(NU, a.n_runs - run0);
   float (*zs)[kZS] = sm.zs;
   float (*cm)[kCS] = sm.cm;
   float* wch = sm.wch;
@@ -250,17 +281,21 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
   float* cuuz = sm.cuuz;
   unsigned short* mww_pr = sm.mww_pr;
 
-  // rows d..15 of the staging area stay zero; (p, r) of the walk moments
-  for (int e = d * kZS + lane; e < 16 * kZS; e += 32) (&zs[0][0])[e] = 0.f;
+  // staging rows without a feature stay zero; (p, r) of the walk moments
+  for (int e = lane; e < 16 * kZS; e += 32) {
+    const int row = e / kZS;
+    if ((PAIR ? (row & 7) : row) >= d) (&zs[0][0])[e] = 0.f;
+  }
   for (int e = lane; e < NMWW; e += 32) {
     int t = e, aa = 0;
     while (t >= d - aa) { t -= d - aa; aa++; }
     mww_pr[e] = (unsigned short)(aa | ((aa + t) << 8));
   }
-  // G-row coefficients: value = c[0]*b + c[1] + c[2]*u + c[3]*u^2
+  // G-row coefficients: value = c[0]*b + c[1] + c[2]*u + c[3]*u^2 (packed: the
+  // lane's rows g and g + 8 are local row g of runs A and B)
   float cA[4], cB[4];
   {
-    const int r[2] = {g, g + 8};
+    const int r[2] = {g, PAIR ? g : g + 8};
     for (int h = 0; h < 2; h++) {
       float* cc = h ? cB : cA;
       const int rr = r[h];
@@ -273,8 +308,8 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
   const int T = a.steps, L = a.chunk;
   const float invL = 1.0f / (float)L;
   const float invTf = 1.0f / (float)T;
-  const uint32_t seed = a.seed_first + (uint32_t)run;
-  for (int e = lane; e < NREC; e += 32) {
+  const uint32_t seed0 = a.seed_first + (uint32_t)run0;
+  for (int e = lane; e < NU * NREC; e += 32) {
     rech[e] = 0.f;
     recl[e] = 0.f;
   }
@@ -297,25 +332,30 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
     float chiA = 0.f, cloA = 0.f, chiB = 0.f, cloB = 0.f;
 
     for (int t0 = c0; t0 < c0 + Lc; t0 += 32) {
-      // producer: lane = tile step, all d increments of column t0 + lane
+      // producer: lane = tile step, all d increments of column t0 + lane of each run
       const int i = t0 + lane;
       const bool valid = i < T;
-      if (EXT) {
-        const double* src = a.ext + ((size_t)run * T + (valid ? i : 0)) * d;
 #pragma unroll
-        for (int f = 0; f < d; f++) zs[f][lane] = valid ? (float)(src[f] * a.ext_inv_scale) : 0.f;
-      } else {
+      for (int r = 0; r < NU; r++) {
+        const int row0 = 8 * r;
+        if (EXT) {
+          const bool ok = valid && r < nrun;
+          const double* src = a.ext + ((size_t)(run0 + (ok ? r : 0)) * T + (ok ? i : 0)) * d;
 #pragma unroll
-        for (int j = 0; j < NQ; j++) {
-          float z[4];
-          jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed, rk, z);
+          for (int f = 0; f < d; f++) zs[row0 + f][lane] = ok ? (float)(src[f] * a.ext_inv_scale) : 0.f;
+        } else {
 #pragma unroll
-          for (int e = 0; e < 4; e++)
-            if (4 * j + e < d) zs[4 * j + e][lane] = z[e];
+          for (int j = 0; j < NQ; j++) {
+            float z[4];
+            jne_normal_quad((uint32_t)(i + 1), (uint32_t)j, seed0 + (uint32_t)r, rk, z);
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+              if (4 * j + e < d) zs[row0 + 4 * j + e][lane] = z[e];
+          }
+          if (!valid)
+#pragma unroll
+            for (int f = 0; f < d; f++) zs[row0 + f][lane] = 0.f;
         }
-        if (!valid)
-#pragma unroll
-          for (int f = 0; f < d; f++) zs[f][lane] = 0.f;
       }
       __syncwarp();
       const int nvalid = min(32, T - t0);
@@ -327,28 +367,40 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
       __syncwarp();
     }
 
-    // ---- chunk end: stage the local Gram (cm[row][col], col < 16: walk column,
-    //      16 + f: increment f) and the chunk totals ----
+    // ---- chunk end: stage the local Gram (cm[row][col]; row 8 r + local row of
+    //      run r when packed; col < 16: walk column, 16 + f: increment f) and the
+    //      chunk totals ----
+    if (PAIR) {
+      cm[g][2 * q] = acc[0][0] + accx[0][0];          // run A: block 0, rows 0..7
+      cm[g][2 * q + 1] = acc[0][1] + accx[0][1];
+      cm[g + 8][2 * q] = acc[1][2] + accx[1][2];      // run B: block 1, rows 8..15
+      cm[g + 8][2 * q + 1] = acc[1][3] + accx[1][3];
+      const int zr = q < 2 ? g : g + 8, zc = 16 + 2 * (q & 1);  // block 2: [z of A | z of B]
+      cm[zr][zc] = (q < 2 ? acc[2][0] + accx[2][0] : acc[2][2] + accx[2][2]);
+      cm[zr][zc + 1] = (q < 2 ? acc[2][1] + accx[2][1] : acc[2][3] + accx[2][3]);
+    } else {
 #pragma unroll
-    for (int n = 0; n < 3; n++) {
-      if (n == 1 && DIM <= 8) continue;
-      const int col = n == 0 ? 2 * q : n == 2 ? 16 + 2 * q : (q < 2 ? 8 + 2 * q : 20 + 2 * q);
-      cm[g][col] = acc[n][0] + accx[n][0];
-      cm[g][col + 1] = acc[n][1] + accx[n][1];
-      cm[g + 8][col] = acc[n][2] + accx[n][2];
-      cm[g + 8][col + 1] = acc[n][3] + accx[n][3];
+      for (int n = 0; n < 3; n++) {
+        if (n == 1 && DIM <= 8) continue;
+        const int col = n == 0 ? 2 * q : n == 2 ? 16 + 2 * q : (q < 2 ? 8 + 2 * q : 20 + 2 * q);
+        cm[g][col] = acc[n][0] + accx[n][0];
+        cm[g][col + 1] = acc[n][1] + accx[n][1];
+        cm[g + 8][col] = acc[n][2] + accx[n][2];
+        cm[g + 8][col + 1] = acc[n][3] + accx[n][3];
+      }
     }
     if (q == 0) {
       if (g < d) two_sum(chiA, cloA, tzh[g], tzl[g]);
-      if (g + 8 < d) two_sum(chiB, cloB, tzh[g + 8], tzl[g + 8]);
+      if (PAIR ? g < d : g + 8 < d) two_sum(chiB, cloB, tzh[g + 8], tzl[g + 8]);
     }
     __syncwarp();
-    // ---- merge into the run's record: W = m + beta (m = chunk mean of W, sum beta = 0),
+    // ---- merge into the runs' records: W = m + beta (m = chunk mean of W, sum beta = 0),
     //      y = ybar + h (u - ubar).  Every moment splits into a "mean" part, a product of
     //      chunk means (float-float), and a centred local part (FP32, small); both are
     //      summed across chunks in float-float.  No FP64 instruction: on this GPU one warp's
     //      FP64 instruction holds the FP64 pipe for ~75 cycles, and the merge would be
-    //      bound by it on short chunks. ----
+    //      bound by it on short chunks.  Per-feature values of run r live at index
+    //      8 r + f. ----
     const jne_chunk_time ct = a.chunk_tab[c0 / L];
     const float Lcf = (float)Lc, invLcf = 1.0f / Lcf;
     const float P1f = 0.5f * Lcf * (Lcf - 1.0f) * invL;
@@ -357,83 +409,93 @@ __device__ __forceinline__ void accum_run(const jne_accum_args& a, int run, Warp
     const float sig2 = P2f - P1f * ub;             // sum of (u - ubar)^2
     const float qbar = sig2 * invLcf;              // mean of (u - ubar)^2
     const float hf = (float)L * invTf, ybf = ct.ybar_hi;
-    if (lane < d) {
-      const int f = lane;
-      const float Sb = cm[d][f], Sub = cm[d + 1][f], Suub = cm[d + 2][f];
-      const float Suz = cm[d + 1][16 + f], Suuz = cm[d + 2][16 + f];
+    const int lf = PAIR ? (lane & 7) : lane, lr0 = PAIR ? (lane & 8) : 0;  // lane's feature and its run's row 0
+    const bool lane_feature = lane_feature_of<DIM>(lane);
+    if (lane_feature) {
+      const int f = lf, x = lane;
+      const float Sb = cm[lr0 + d][f], Sub = cm[lr0 + d + 1][f], Suub = cm[lr0 + d + 2][f];
+      const float Suz = cm[lr0 + d + 1][16 + f], Suuz = cm[lr0 + d + 2][16 + f];
       // m = wc + Sb / Lc: the quotient with its exact remainder
       const float qh = __fmul_rn(Sb, ct.inv_lc);
       const float ql = __fmul_rn(__fmaf_rn(-qh, ct.lc, Sb), ct.inv_lc);
-      float mh = wch[f], ml = wcl[f];
+      float mh = wch[x], ml = wcl[x];
       ff_acc(mh, ml, qh, ql);
-      mmh[f] = mh;
-      mml[f] = ml;
+      mmh[x] = mh;
+      mml[x] = ml;
       float ph, pe;
       ff_mul(mh, ml, ct.lc, 0.f, ph, pe);
       float lh, ll = 0.f;
       two_sum(ph, pe, lh, ll);
-      lmh[f] = lh;
-      lml[f] = ll;
-      const float tzf = tzh[f];
-      sbf[f] = Sb;
-      tzfs[f] = tzf;
-      cub[f] = Sub - ub * Sb;                                              // sum (u-ubar) beta
-      cuub[f] = Suub - 2.0f * ub * Sub + ub * ub * Sb - Sb * invLcf * sig2;  // sum (u-ubar)^2 beta
-      cuz[f] = Suz - ub * tzf;                                             // sum (u-ubar) z
-      cuuz[f] = Suuz - 2.0f * ub * Suz + ub * ub * tzf - qbar * tzf;       // sum ((u-ubar)^2 - qbar) z
+      lmh[x] = lh;
+      lml[x] = ll;
+      const float tzf = tzh[x];
+      sbf[x] = Sb;
+      tzfs[x] = tzf;
+      cub[x] = Sub - ub * Sb;                                              // sum (u-ubar) beta
+      cuub[x] = Suub - 2.0f * ub * Sub + ub * ub * Sb - Sb * invLcf * sig2;  // sum (u-ubar)^2 beta
+      cuz[x] = Suz - ub * tzf;                                             // sum (u-ubar) z
+      cuuz[x] = Suuz - 2.0f * ub * Suz + ub * ub * tzf - qbar * tzf;       // sum ((u-ubar)^2 - qbar) z
     }
     __syncwarp();
     // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy.
     // One loop per slot kind, so the lanes of an iteration take one path.
     const float c1y = hf, c2y = 2.0f * ybf * hf, c2yy = hf * hf;  // y and y^2 coefficients
-    for (int e = lane; e < NMWW; e += 32) {
-      const int p = mww_pr[e] & 0xff, r = mww_pr[e] >> 8;
+    for (int t = lane; t < NU * NMWW; t += 32) {
+      const int r = t / NMWW, e = t - r * NMWW, o = 8 * r;
+      const int p = o + (mww_pr[e] & 0xff), c = mww_pr[e] >> 8;
       float ph, pe;
-      ff_mul(lmh[p], lml[p], mmh[r], mml[r], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, cm[p][r] - sbf[p] * sbf[r] * invLcf));
+      ff_mul(lmh[p], lml[p], mmh[o + c], mml[o + c], ph, pe);
+      ff_acc(rech[r * NREC + e], recl[r * NREC + e], ph,
+             __fadd_rn(pe, cm[p][c] - sbf[p] * sbf[o + c] * invLcf));
     }
-    for (int t = lane; t < NMW; t += 32) {
-      const int pp = t / d, r = t - pp * d, e = NMWW + t;
+    for (int t = lane; t < NU * NMW; t += 32) {
+      const int r = t / NMW, tt = t - r * NMW, pp = tt / d, x = 8 * r + tt - pp * d, e = r * NREC + NMWW + tt;
       const float wh = pp == 0 ? 1.f : pp == 1 ? ct.ybar_hi : ct.y2bar_hi;
       const float wl = pp == 0 ? 0.f : pp == 1 ? ct.ybar_lo : ct.y2bar_lo;
       const float a1 = pp == 0 ? 0.f : pp == 1 ? c1y : c2y, a2 = pp == 2 ? c2yy : 0.f;
       float ph, pe;
-      ff_mul(wh, wl, lmh[r], lml[r], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cub[r] + a2 * cuub[r]));
+      ff_mul(wh, wl, lmh[x], lml[x], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cub[x] + a2 * cuub[x]));
     }
-    for (int t = lane; t < NNZW; t += 32) {
-      const int za = t / d, wb = t - za * d, e = NMWW + NMW + t;
+    for (int t = lane; t < NU * NNZW; t += 32) {
+      const int r = t / NNZW, tt = t - r * NNZW, za = tt / d, wb = tt - za * d, o = 8 * r;
+      const int e = r * NREC + NMWW + NMW + tt;
       float ph, pe;
-      ff_mul(tzh[za], tzl[za], mmh[wb], mml[wb], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, cm[wb][16 + za] - tzfs[za] * sbf[wb] * invLcf));
+      ff_mul(tzh[o + za], tzl[o + za], mmh[o + wb], mml[o + wb], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, cm[o + wb][16 + za] - tzfs[o + za] * sbf[o + wb] * invLcf));
     }
-    for (int t = lane; t < 2 * d; t += 32) {
-      const int pp = t / d, za = t - pp * d, e = NMWW + NMW + NNZW + d + t;
+    for (int t = lane; t < NU * 2 * d; t += 32) {
+      const int r = t / (2 * d), tt = t - r * 2 * d, pp = tt / d, x = 8 * r + tt - pp * d;
+      const int e = r * NREC + NMWW + NMW + NNZW + d + tt;
       const float wh = pp == 0 ? ct.ybar_hi : ct.y2bar_hi, wl = pp == 0 ? ct.ybar_lo : ct.y2bar_lo;
       const float a1 = pp == 0 ? c1y : c2y, a2 = pp == 0 ? 0.f : c2yy;
       float ph, pe;
-      ff_mul(wh, wl, tzh[za], tzl[za], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cuz[za] + a2 * cuuz[za]));
+      ff_mul(wh, wl, tzh[x], tzl[x], ph, pe);
+      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cuz[x] + a2 * cuuz[x]));
     }
     __syncwarp();
-    if (lane < d) ff_acc(wch[lane], wcl[lane], tzh[lane], tzl[lane]);
+    if (lane_feature) ff_acc(wch[lane], wcl[lane], tzh[lane], tzl[lane]);
     __syncwarp();
   }
 
-  // ---- write the record (slot order of jne_common.cuh) in FP64 ----
-  if (lane < d) {
-    rech[jne_slot_Nz1(lane, d)] = wch[lane];
-    recl[jne_slot_Nz1(lane, d)] = wcl[lane];
+  // ---- write the records (slot order of jne_common.cuh) in FP64 ----
+  if (lane_feature_of<DIM>(lane)) {
+    const int r = PAIR ? lane >> 3 : 0, f = PAIR ? (lane & 7) : lane;
+    rech[r * NREC + jne_slot_Nz1(f, d)] = wch[lane];
+    recl[r * NREC + jne_slot_Nz1(f, d)] = wcl[lane];
   }
   __syncwarp();
   const size_t ld = (size_t)a.mom_ld;
-  for (int e = lane; e < NREC; e += 32) a.mom[(size_t)e * ld + run] = (double)rech[e] + (double)recl[e];
+  for (int t = lane; t < NU * NREC; t += 32) {
+    const int r = t / NREC, e = t - r * NREC;
+    if (r < nrun) a.mom[(size_t)e * ld + run0 + r] = (double)rech[t] + (double)recl[t];
+  }
   __syncwarp();
 }
 
-// Fused finalize.  Runs are counted per batch of 32 consecutive items; the
-// warp that accumulates the last run of a batch finalizes the whole batch, one
-// run per lane, in FP64 -- a pipe the accumulation leaves idle, so the
+// Fused finalize.  Units (runs, or packed pairs of runs) are counted per batch
+// of 32 consecutive items; the warp that accumulates the last unit of a batch
+// finalizes the whole batch, one unit per lane, in FP64 -- a pipe the accumulation leaves idle, so the
 // finalize runs in the shadow of the other warps' accumulation instead of in a
 // second kernel after it.  Every batch is full except the very last, and a
 // lane's record reads are contiguous with its neighbours'.  Ordering: the
@@ -454,7 +516,22 @@ __device__ __forceinline__ long long batch_complete(unsigned int* batch_done, lo
   return first;
 }
 
-// One request: every warp strides over its runs.  The round keys arrive as a
+// Units of a request of n runs: runs, or pairs of runs for packed dims.
+template <int DIM>
+__host__ __device__ __forceinline__ long long unit_count(long long n_runs) {
+  return jne_units(DIM, n_runs);
+}
+
+// The finalize of one unit's runs (one, or a packed pair).
+__device__ __forceinline__ void finalize_unit(const jne_finalize_args& fin, long long unit) {
+  const int nu = fin.dim <= JNE_PACK_MAX_DIM ? 2 : 1;
+  for (int r = 0; r < nu; r++) {
+    const long long run = nu * unit + r;
+    if (run < fin.n_runs) jne_fin::finalize_run(fin, (int)run);
+  }
+}
+
+// One request: every warp strides over its units.  The round keys arrive as a
 // kernel parameter (computed on the host): the Philox rounds read them from
 // the parameter bank instead of holding 20 registers.  With fin.out set, the
 // kernel also finalizes its runs (fin describes the same request).
@@ -466,31 +543,33 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nwarps = gridDim.x * kMixWarps;
   const bool fused = fin.out != nullptr && a.batch_done != nullptr;
-  auto finalize_batch = [&](int run) {
-    const long long first = batch_complete(a.batch_done, run, a.n_runs, lane);
-    if (first >= 0 && first + lane < a.n_runs) jne_fin::finalize_run(fin, (int)(first + lane));
+  const long long units = unit_count<DIM>(a.n_runs);
+  auto finalize_batch = [&](long long unit) {
+    const long long first = batch_complete(a.batch_done, unit, units, lane);
+    if (first >= 0 && first + lane < units) finalize_unit(fin, first + lane);
     __syncwarp();
   };
   if (a.next_run == nullptr) {
-    for (int run = blockIdx.x * kMixWarps + wib; run < a.n_runs; run += nwarps) {
-      accum_run<DIM, EXT>(a, run, sm_all[wib], rk, lane);
-      if (fused) finalize_batch(run);
+    for (long long unit = blockIdx.x * kMixWarps + wib; unit < units; unit += nwarps) {
+      accum_unit<DIM, EXT>(a, (int)unit, sm_all[wib], rk, lane);
+      if (fused) finalize_batch(unit);
     }
   } else {
-    // first run by warp index, then the next free one from the counter
-    for (long long run = blockIdx.x * kMixWarps + wib; run < a.n_runs;) {
-      accum_run<DIM, EXT>(a, (int)run, sm_all[wib], rk, lane);
-      if (fused) finalize_batch((int)run);
+    // first unit by warp index, then the next free one from the counter
+    for (long long unit = blockIdx.x * kMixWarps + wib; unit < units;) {
+      accum_unit<DIM, EXT>(a, (int)unit, sm_all[wib], rk, lane);
+      if (fused) finalize_batch(unit);
       unsigned long long item = 0;
       if (lane == 0) item = atomicAdd(a.next_run, 1ull);
-      run = nwarps + (long long)__shfl_sync(0xffffffffu, item, 0);
+      unit = nwarps + (long long)__shfl_sync(0xffffffffu, item, 0);
     }
   }
 }
 
 // A ragged batch of requests (any dims, step counts and sizes) in one
-// persistent launch: each warp takes the next run of the flattened batch from
+// persistent launch: each warp takes the next unit of the flattened batch from
 // a global counter, so long and short requests share the GPU without tails.
+// reqs[r].first counts units.
 __device__ __forceinline__ int request_of(const jne_ragged_req* __restrict__ reqs, int n_req, long long item) {
   int lo = 0, hi = n_req - 1;  // request r with reqs[r].first <= item < reqs[r + 1].first
   while (lo < hi) {
@@ -514,35 +593,34 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
     if (item >= (unsigned long long)total) break;
     const int lo = request_of(reqs, n_req, (long long)item);
     const jne_accum_args& a = reqs[lo].acc;
-    const int run = (int)(item - (unsigned long long)reqs[lo].first);
+    const int unit = (int)(item - (unsigned long long)reqs[lo].first);
     const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
     switch (a.dim) {
-      case 1: accum_run<1, false>(a, run, sm_all[wib], rk, lane); break;
-      case 2: accum_run<2, false>(a, run, sm_all[wib], rk, lane); break;
-      case 3: accum_run<3, false>(a, run, sm_all[wib], rk, lane); break;
-      case 4: accum_run<4, false>(a, run, sm_all[wib], rk, lane); break;
-      case 5: accum_run<5, false>(a, run, sm_all[wib], rk, lane); break;
-      case 6: accum_run<6, false>(a, run, sm_all[wib], rk, lane); break;
-      case 7: accum_run<7, false>(a, run, sm_all[wib], rk, lane); break;
-      case 8: accum_run<8, false>(a, run, sm_all[wib], rk, lane); break;
-      case 9: accum_run<9, false>(a, run, sm_all[wib], rk, lane); break;
-      case 10: accum_run<10, false>(a, run, sm_all[wib], rk, lane); break;
-      case 11: accum_run<11, false>(a, run, sm_all[wib], rk, lane); break;
-      default: accum_run<12, false>(a, run, sm_all[wib], rk, lane); break;
+      case 1: accum_unit<1, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 2: accum_unit<2, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 3: accum_unit<3, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 4: accum_unit<4, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 5: accum_unit<5, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 6: accum_unit<6, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 7: accum_unit<7, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 8: accum_unit<8, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 9: accum_unit<9, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 10: accum_unit<10, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 11: accum_unit<11, false>(a, unit, sm_all[wib], rk, lane); break;
+      default: accum_unit<12, false>(a, unit, sm_all[wib], rk, lane); break;
     }
     if (batch_done) {
       const long long first = batch_complete(batch_done, (long long)item, total, lane);
       if (first >= 0 && first + lane < total) {
         const int r = request_of(reqs, n_req, first + lane);
-        jne_fin::finalize_run(reqs[r].fin, (int)(first + lane - reqs[r].first));
+        finalize_unit(reqs[r].fin, first + lane - reqs[r].first);
       }
       __syncwarp();
     }
   }
 }
 
-// Persistent grid: exactly the resident blocks (so every warp strides over the
-// same number of runs, +-1), or fewer when the batch is small.
+// Persistent grid: exactly the resident blocks, or fewer when the batch is small.
 template <typename K>
 int resident_grid(K kernel, int threads, size_t shm, int sms, long long n_runs, int warps_per_block) {
   int per_sm = 0;
@@ -559,10 +637,10 @@ cudaError_t launch_dim(const jne_accum_args& a, const jne_finalize_args& fin, in
   const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
   if (a.ext) {
     auto k = k_accum_mixed<DIM, true>;
-    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk, fin);
+    k<<<resident_grid(k, threads, 0, sms, unit_count<DIM>(a.n_runs), kMixWarps), threads, 0, st>>>(a, rk, fin);
   } else {
     auto k = k_accum_mixed<DIM, false>;
-    k<<<resident_grid(k, threads, 0, sms, a.n_runs, kMixWarps), threads, 0, st>>>(a, rk, fin);
+    k<<<resident_grid(k, threads, 0, sms, unit_count<DIM>(a.n_runs), kMixWarps), threads, 0, st>>>(a, rk, fin);
   }
   return cudaGetLastError();
 }

@@ -73,7 +73,7 @@ void describe(jne_context* c, const jne_request* reqs, double* const* outs, cons
     d.fin.status = c->d_status;
     d.first = first;
     fill_chunk_table(r.steps, chunk, ht + toff);
-    first += p.n;
+    first += jne_units(r.dim, p.n);  // the kernel's items are units (packed pairs for small dims)
     moff += (size_t)p.n * jne_record_slots(r.dim);
     toff += (size_t)nch;
   }
@@ -106,9 +106,10 @@ std::vector<std::vector<Piece>> plan_launches(const jne_request* reqs, const std
   return out;
 }
 
-long long total_runs(const std::vector<Piece>& pieces) {
+// Items of a ragged launch: units, i.e. runs, or pairs of runs for packed dims.
+long long total_units(const jne_request* reqs, const std::vector<Piece>& pieces) {
   long long n = 0;
-  for (const Piece& p : pieces) n += p.n;
+  for (const Piece& p : pieces) n += jne_units(reqs[p.req].dim, p.n);
   return n;
 }
 
@@ -187,7 +188,8 @@ int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* co
         (rc = ensure(c, &c->d_reqs[b], &c->reqs_cap[b], pieces.size(), "request table")) ||
         (rc = ensure(c, &c->d_rtab[b], &c->rtab_cap[b], ntab, "chunk tables")) ||
         (rc = ensure(c, &c->d_counter[b], &c->counter_cap[b], 1, "work counter")) ||
-        (rc = ensure(c, &c->d_bdone[b], &c->bdone_cap[b], ((size_t)total_runs(pieces) + 31) / 32, "batch counts")) ||
+        (rc = ensure(c, &c->d_bdone[b], &c->bdone_cap[b], ((size_t)total_units(reqs, pieces) + 31) / 32,
+                     "batch counts")) ||
         (rc = ensure_pinned(c, &c->h_reqs[b], &c->h_reqs_cap[b], pieces.size())) ||
         (rc = ensure_pinned(c, &c->h_rtab[b], &c->h_rtab_cap[b], ntab)))
       return rc;
@@ -236,7 +238,7 @@ int jne_plan_create(jne_context* c, const jne_request* reqs, int n_req, double* 
     slots += (size_t)reqs[i].n_runs * jne_record_slots(reqs[i].dim);
   }
   const size_t ntab = chunks_of(c, reqs, pieces);
-  const size_t nbatch = ((size_t)total_runs(pieces) + 31) / 32;
+  const size_t nbatch = ((size_t)total_units(reqs, pieces) + 31) / 32;
   const unsigned long long bytes = slots * sizeof(double) + pieces.size() * sizeof(jne_ragged_req) +
                                    ntab * sizeof(jne_chunk_time) + sizeof(unsigned long long) +
                                    nbatch * sizeof(unsigned int);

@@ -8,6 +8,13 @@ struct jne_time_sums {
   double Y[5];
 };
 
+// The mixed kernels pack two runs into one warp ("unit") for dims up to this:
+// a request of n runs is ceil(n / 2) units, else n.
+#define JNE_PACK_MAX_DIM 4
+__host__ __device__ __forceinline__ long long jne_units(int dim, long long n_runs) {
+  return dim <= JNE_PACK_MAX_DIM ? (n_runs + 1) / 2 : n_runs;
+}
+
 // Argument block of the finalize kernel.
 struct jne_finalize_args {
   int model, dim, steps, n_runs;
