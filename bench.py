@@ -529,7 +529,7 @@ def main() -> None:
     ap.add_argument("--err-runs", type=int, default=2_000)
     ap.add_argument("--cpu-runs", type=int, default=None, help="CPU sample runs per model (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length without --cpu-runs")
-    ap.add_argument("--chunk", type=int, default=0, help="steps per FP32 chunk (0: adaptive, 256 at T=10k)")
+    ap.add_argument("--chunk", type=int, default=0, help="steps per FP32 chunk (0: adaptive, 512 at T=10k)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per accumulation launch (default: the committed capture, scaled by runs)")
     ap.add_argument("--ragged-steps", type=int, default=2, help="timed replays of the ragged 60-pair plan (0: skip)")

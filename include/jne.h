@@ -72,7 +72,7 @@ void jne_close(jne_context* ctx);
 const char* jne_last_error(const jne_context* ctx);
 
 /* Steps per FP32 chunk of the mixed kernel: a multiple of 32, or 0 (the
- * default) for about steps/32 rounded down to a power of two in [32, 256], or
+ * default) for the largest power of two <= steps/16 in [32, 512], or
  * JNE_CHUNK_TUNED for the lengths jne_autotune_chunk chose (the default rule
  * for classes it has not tuned). */
 #define JNE_CHUNK_TUNED (-1)
@@ -132,7 +132,7 @@ int jne_eigs_seeded_models(jne_context* ctx, const int* models, int n_models, in
  * allocating library routine.  Results go to out_device (n_runs x k doubles)
  * on `stream` (a cudaStream_t; null = the legacy default stream); the call
  * waits for them.  At most JNE_NOALLOC_MAX_RUNS runs per call (and, for mixed
- * precision, at most JNE_NOALLOC_MAX_CHUNKS chunks: 1,048,576 steps), else
+ * precision, at most JNE_NOALLOC_MAX_CHUNKS chunks: 2,097,152 steps), else
  * JNE_ERR_BUDGET.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  All calls share the one array, so calls

@@ -30,7 +30,14 @@ constexpr int kMixWarps = 4;
 constexpr int kZS = 36;  // z staging row stride (floats): conflict-free float4 reads
 constexpr int kCS = 33;  // chunk-Gram staging row stride (floats)
 
-__device__ __forceinline__ uint32_t tf32_hi(float x) { return __float_as_uint(x) & 0xFFFFE000u; }
+// x rounded to the nearest TF32 value (ties away from zero): the low 13
+// mantissa bits are zero, and x - hi is exact in FP32 with |x - hi| <= 2^-12 |x|
+// -- half the remainder of truncation, so the remainder keeps one more bit
+// when the tensor core truncates it to TF32 in turn.
+// (Integer form: add half a TF32 ulp to the magnitude bits, clear the low 13;
+// a carry into the exponent is the correct rounding.  Cheaper here than the
+// conversion instruction.)
+__device__ __forceinline__ uint32_t tf32_hi(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
 
 __device__ __forceinline__ void mma_tf32(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint32_t b0, uint32_t b1) {

@@ -46,10 +46,11 @@ int fail(int code, const std::string& m) {
 }
 
 // Same policy as the context entry points: mixed requests on short paths run
-// the FP64 kernel, and the mixed chunk length is about steps/32 in [32, 256].
+// the FP64 kernel, and the mixed chunk length is the largest power of two
+// <= steps/16 in [32, 512].
 int noalloc_chunk(int steps) {
   int L = 32;
-  while (L < 256 && 2 * L * 32 <= steps) L *= 2;
+  while (L < 512 && 2 * L * 16 <= steps) L *= 2;
   return L;
 }
 
@@ -115,7 +116,7 @@ extern "C" int jne_eigs_seeded_noalloc(int device, int model, int dim, int steps
   const int nch = (steps + chunk - 1) / chunk;
   if (mixed && nch > JNE_NOALLOC_MAX_CHUNKS)
     return fail(JNE_ERR_BUDGET, "steps " + std::to_string(steps) + " exceed the no-allocation limit of " +
-                                    std::to_string(JNE_NOALLOC_MAX_CHUNKS * 256) + " steps for mixed precision");
+                                    std::to_string(JNE_NOALLOC_MAX_CHUNKS * 512) + " steps for mixed precision");
   if ((uint64_t)seed_first + (uint64_t)n_runs > 0x100000000ull) return fail(JNE_ERR_ARG, "seed range exceeds u32");
   if (n_runs == 0) return JNE_OK;
   if (!out_device) return fail(JNE_ERR_ARG, "null output buffer");
