@@ -39,9 +39,9 @@ UNIT = "runs/s"
 
 # DRAM bytes (read + write) of one k_accum_mixed<12> launch (accumulation + fused
 # finalize) per run, from an ncu capture of the full 200,000-run launch
-# (profiles/k_accum_mixed_dim12_T10k_dram.md): 27,513,856 B read + 966,693,120 B written.
+# (profiles/k_accum_mixed_dim12_T10k_dram.md): 32,463,360 B read + 988,989,952 B written.
 # Algorithmic: 2,352 B of record written and read back, 96 B of eigenvalues per run.
-ACCUM_DRAM_BYTES_PER_RUN = (27_513_856 + 966_693_120) / 200_000
+ACCUM_DRAM_BYTES_PER_RUN = (32_463_360 + 988_989_952) / 200_000
 
 
 def k_of(model: int) -> int:
