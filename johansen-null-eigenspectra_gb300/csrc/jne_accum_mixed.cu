@@ -12,9 +12,10 @@
 // warp accumulates, in FP32 on the tensor cores, the 16 x 32 local Gram
 //     sum_tau G_tau [G_tau; z_tau]',   G = [b (d rows); 1; u; u^2; 0...],
 // with u = tau / chunk.  Each operand is split x = hi + lo with hi = x rounded
-// down to TF32 (19 bits) and every product is hi*hi + hi*lo + lo*hi (three
-// MMAs).  At the chunk end the local Gram is mapped to the global FP64 moments
-// (W = Wc + b, y = yc + h u) by the exact shift identities, in FP64.
+// to the nearest TF32 value (19 bits) and every product is hi*hi + hi*lo +
+// lo*hi (three MMAs).  At the chunk end the local Gram is mapped to the global
+// moments (W = Wc + b, y = yc + h u) by the exact shift identities, summed in
+// float-float; the record is written in FP64 once per run.
 //
 // Fragment layout (PTX ISA, mma.m16n8k8 .tf32): lane (g = lane/4, q = lane%4)
 // holds rows g and g+8 of A at k-slots q and q+4, and column g of B at the same
@@ -58,26 +59,43 @@ __device__ __forceinline__ void mma_tf32_first(float (&d)[4], uint32_t a0, uint3
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1), "f"(0.0f));
 }
 
-// A B with A, B given as float values, on the TF32 split: the hi*hi product
-// goes to `hh` (overwritten when FIRST), the two cross products to `x`.  The tensor core's FP32
-// accumulation truncates, so its error is biased and grows with the number of
-// additions into one accumulator: keeping the (2^11 times smaller) cross terms
-// apart and emptying `hh` after every tile keeps that bias ~10x below a single
-// accumulator per chunk.
+// x - y on a pair of floats in one instruction (each half rounded as the
+// scalar subtraction).
+__device__ __forceinline__ float2 sub_pair(float2 x, float2 y) {
+  unsigned long long ux, uy, r;
+  asm("mov.b64 %0, {%1,%2};" : "=l"(ux) : "f"(x.x), "f"(x.y));
+  asm("mov.b64 %0, {%1,%2};" : "=l"(uy) : "f"(y.x), "f"(y.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(ux), "l"(uy));
+  float2 d;
+  asm("mov.b64 {%0,%1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(r));
+  return d;
+}
+
+// The TF32 split of a pair: hi = each value rounded to TF32, lo = x - hi (exact).
+__device__ __forceinline__ void split_pair(float2 x, uint32_t& h0, uint32_t& h1, uint32_t& l0, uint32_t& l1) {
+  h0 = tf32_hi(x.x);
+  h1 = tf32_hi(x.y);
+  const float2 lo = sub_pair(x, make_float2(__uint_as_float(h0), __uint_as_float(h1)));
+  l0 = __float_as_uint(lo.x);
+  l1 = __float_as_uint(lo.y);
+}
+
+// C += A B on the TF32 split, A (a0..a3) and B (b0, b1) given as hi and lo
+// words: the hi*hi product goes to `hh` (overwritten when FIRST), the two cross
+// products to `x`.  The tensor core's FP32 accumulation truncates, so its
+// error is biased and grows with the number of additions into one accumulator:
+// keeping the (2^11 times smaller) cross terms apart and emptying `hh` after
+// every tile keeps that bias ~10x below a single accumulator per chunk.
 template <bool FIRST>
-__device__ __forceinline__ void mma_split(float (&hh)[4], float (&x)[4], float a0, float a1, float a2, float a3,
-                                          float b0, float b1) {
-  const uint32_t ah0 = tf32_hi(a0), ah1 = tf32_hi(a1), ah2 = tf32_hi(a2), ah3 = tf32_hi(a3);
-  const uint32_t bh0 = tf32_hi(b0), bh1 = tf32_hi(b1);
-  const uint32_t al0 = __float_as_uint(a0 - __uint_as_float(ah0)), al1 = __float_as_uint(a1 - __uint_as_float(ah1));
-  const uint32_t al2 = __float_as_uint(a2 - __uint_as_float(ah2)), al3 = __float_as_uint(a3 - __uint_as_float(ah3));
-  const uint32_t bl0 = __float_as_uint(b0 - __uint_as_float(bh0)), bl1 = __float_as_uint(b1 - __uint_as_float(bh1));
-  mma_tf32(x, al0, al1, al2, al3, bh0, bh1);
-  mma_tf32(x, ah0, ah1, ah2, ah3, bl0, bl1);
+__device__ __forceinline__ void mma_split(float (&hh)[4], float (&x)[4], const uint32_t (&ah)[4],
+                                          const uint32_t (&al)[4], uint32_t bh0, uint32_t bh1, uint32_t bl0,
+                                          uint32_t bl1) {
+  mma_tf32(x, al[0], al[1], al[2], al[3], bh0, bh1);
+  mma_tf32(x, ah[0], ah[1], ah[2], ah[3], bl0, bl1);
   if (FIRST)
-    mma_tf32_first(hh, ah0, ah1, ah2, ah3, bh0, bh1);
+    mma_tf32_first(hh, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
   else
-    mma_tf32(hh, ah0, ah1, ah2, ah3, bh0, bh1);
+    mma_tf32(hh, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
 }
 
 // Two-sum carry update: (hi, lo) += t.
@@ -213,21 +231,34 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   if (!BLOCK1)
 #pragma unroll
     for (int r = 0; r < 4; r++) hh[1][r] = 0.f;
-  mma_split<true>(hh[0], accx[0], GA[0], GB[0], GA[1], GB[1], GA[0], GA[1]);
-  if (BLOCK1) mma_split<true>(hh[1], accx[1], GA[0], GB[0], GA[1], GB[1], BB[0], BB[1]);
-  mma_split<true>(hh[2], accx[2], GA[0], GB[0], GA[1], GB[1], zA[0], zA[1]);
 #pragma unroll
-  for (int s = 1; s < 4; s++) {
+  for (int s = 0; s < 4; s++) {
     const int j0 = 2 * s, j1 = 2 * s + 1;
-    mma_split<false>(hh[0], accx[0], GA[j0], GB[j0], GA[j1], GB[j1], GA[j0], GA[j1]);
-    if (BLOCK1) mma_split<false>(hh[1], accx[1], GA[j0], GB[j0], GA[j1], GB[j1], BB[j0], BB[j1]);
-    mma_split<false>(hh[2], accx[2], GA[j0], GB[j0], GA[j1], GB[j1], zA[j0], zA[j1]);
+    // A: rows g, g + 8 at steps j0 (a0, a1) and j1 (a2, a3); block 0's B is rows g of A: (a0, a2)
+    uint32_t ah[4], al[4], b1h0, b1h1, b1l0, b1l1, b2h0, b2h1, b2l0, b2l1;
+    split_pair(make_float2(GA[j0], GB[j0]), ah[0], ah[1], al[0], al[1]);
+    split_pair(make_float2(GA[j1], GB[j1]), ah[2], ah[3], al[2], al[3]);
+    if (BLOCK1) split_pair(make_float2(BB[j0], BB[j1]), b1h0, b1h1, b1l0, b1l1);
+    split_pair(make_float2(zA[j0], zA[j1]), b2h0, b2h1, b2l0, b2l1);
+    if (s == 0) {
+      mma_split<true>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
+      if (BLOCK1) mma_split<true>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
+      mma_split<true>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+    } else {
+      mma_split<false>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
+      if (BLOCK1) mma_split<false>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
+      mma_split<false>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+    }
   }
   // empty the tile's hi*hi accumulator into the chunk sum (round to nearest)
 #pragma unroll
   for (int n = 0; n < 3; n++)
 #pragma unroll
-    for (int r = 0; r < 4; r++) acc[n][r] = __fadd_rn(acc[n][r], hh[n][r]);
+    for (int r = 0; r < 4; r += 2) {
+      const float2 v = __fadd2_rn(make_float2(acc[n][r], acc[n][r + 1]), make_float2(hh[n][r], hh[n][r + 1]));
+      acc[n][r] = v.x;
+      acc[n][r + 1] = v.y;
+    }
 }
 
 // Per-warp shared memory of the accumulation (sized for the largest dim).

@@ -54,12 +54,6 @@ __device__ __forceinline__ void jne_philox4x32_10(uint32_t c0, uint32_t c1, uint
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-// u in (0,1): the top 23 bits m of a word, u = (m + 1/2) 2^-23, built in the
-// mantissa of a float in [1, 2) and shifted down (both steps exact).
-__device__ __forceinline__ float jne_u01(uint32_t x) {
-  return __fsub_rn(__uint_as_float(0x3F800000u | (x >> 9)), 0.99999994039535522f);
-}
-
 // Documented PTX approximations (single hardware instructions, so every kernel
 // that draws a value computes it the same way).
 __device__ __forceinline__ float jne_lg2_approx(float x) {
@@ -85,22 +79,34 @@ __device__ __forceinline__ float jne_cos_approx(float x) {
 
 // Box-Muller pair: r = sqrt(-2 ln u(a)), theta = 2 pi u(b) - pi, z = r (cos, sin).
 // Explicit _rn arithmetic keeps any caller from fusing a step into a different
-// FMA, so the values are identical in every kernel that draws them.
-__device__ __forceinline__ void jne_box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
-  const float l2 = jne_lg2_approx(jne_u01(a));                          // log2(u) < 0
-  const float r = jne_sqrt_approx(__fmul_rn(-1.3862943611198906f, l2));  // -2 ln 2 * log2(u)
-  const float th = __fmaf_rn(jne_u01(b), 6.2831853071795865f, -3.1415926535897932f);
-  z0 = __fmul_rn(r, jne_cos_approx(th));
-  z1 = __fmul_rn(r, jne_sin_approx(th));
-}
-
+// FMA, so the values are identical in every kernel that draws them.  The two
+// pairs of a quad go through the FP32 steps together (the paired
+// add/multiply/FMA instructions of this GPU, each half rounded as its scalar
+// form): half the issue slots for those steps, the same values.
 // The four normals of quad j (features 4j..4j+3) of step s.
 __device__ __forceinline__ void jne_normal_quad(uint32_t s, uint32_t j, uint32_t seed, const jne_round_keys& rk,
                                                 float z[4]) {
   uint32_t w[4];
   jne_philox4x32_10(s, j, seed, 0u, rk, w);
-  jne_box_muller(w[0], w[1], z[0], z[1]);
-  jne_box_muller(w[2], w[3], z[2], z[3]);
+  // u in (0,1) for the radius words (w0, w2) and the angle words (w1, w3): the top
+  // 23 bits m of a word, u = (m + 1/2) 2^-23, built in the mantissa of a float in
+  // [1, 2) and shifted down (both steps exact)
+  const float2 off = make_float2(-0.99999994039535522f, -0.99999994039535522f);
+  const float2 ur = __fadd2_rn(make_float2(__uint_as_float(0x3F800000u | (w[0] >> 9)),
+                                           __uint_as_float(0x3F800000u | (w[2] >> 9))), off);
+  const float2 ua = __fadd2_rn(make_float2(__uint_as_float(0x3F800000u | (w[1] >> 9)),
+                                           __uint_as_float(0x3F800000u | (w[3] >> 9))), off);
+  const float2 m = __fmul2_rn(make_float2(-1.3862943611198906f, -1.3862943611198906f),
+                              make_float2(jne_lg2_approx(ur.x), jne_lg2_approx(ur.y)));  // -2 ln 2 * log2(u)
+  const float r0 = jne_sqrt_approx(m.x), r1 = jne_sqrt_approx(m.y);
+  const float2 th = __ffma2_rn(ua, make_float2(6.2831853071795865f, 6.2831853071795865f),
+                               make_float2(-3.1415926535897932f, -3.1415926535897932f));
+  const float2 z01 = __fmul2_rn(make_float2(r0, r0), make_float2(jne_cos_approx(th.x), jne_sin_approx(th.x)));
+  const float2 z23 = __fmul2_rn(make_float2(r1, r1), make_float2(jne_cos_approx(th.y), jne_sin_approx(th.y)));
+  z[0] = z01.x;
+  z[1] = z01.y;
+  z[2] = z23.x;
+  z[3] = z23.y;
 }
 
 // ---------------------------------------------------------------------------
