@@ -39,9 +39,13 @@ UNIT = "runs/s"
 
 # DRAM bytes (read + write) of one k_accum_mixed<12> launch (accumulation + fused
 # finalize) per run, from an ncu capture of the full 200,000-run launch
-# (profiles/k_accum_mixed_dim12_T10k_dram.md): 32,463,360 B read + 988,989,952 B written.
+# (profiles/k_accum_mixed_dim12_T10k_dram.md): 25,171,968 B read + 949,900,544 B written.
 # Algorithmic: 2,352 B of record written and read back, 96 B of eigenvalues per run.
-ACCUM_DRAM_BYTES_PER_RUN = (32_463_360 + 988_989_952) / 200_000
+ACCUM_DRAM_BYTES_PER_RUN = (25_171_968 + 949_900_544) / 200_000
+# Warp instructions k_accum_mixed<12> issues per run at T = 10,000 (accumulation plus
+# the run's share of its fused finalize batch), from an ncu capture of an 8,192-run
+# launch (profiles/k_accum_mixed_dim12_T10k_8192runs_full.md).
+ACCUM_WARP_INST_PER_RUN = 175_044
 
 
 def k_of(model: int) -> int:
@@ -332,6 +336,18 @@ def run_gpu(args, rank: int, world: int) -> None:
                            "note": "executed split-TF32 mma.sync work (not algorithmic flops) vs the measured "
                                    "mma.sync TF32 rate"}
 
+    # SIMT issue, the kernel's binding limit: one warp instruction per cycle per scheduler
+    # (4 per SM) at the SM clock sampled in the timed region
+    clocks = clk.summary()
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0) * 1e6
+    issue_peak = torch.cuda.get_device_properties(local).multi_processor_count * 4 * sm_hz
+    inst_rate = ACCUM_WARP_INST_PER_RUN * R / (mean_acc_ms * 1e-3)
+    issue["warp_issue"] = {"achieved_inst_per_s": inst_rate, "peak_inst_per_s": issue_peak,
+                           "frac": inst_rate / issue_peak if issue_peak else None,
+                           "inst_per_run": ACCUM_WARP_INST_PER_RUN,
+                           "note": "warp instructions per run (ncu) x runs/s of the timed launches vs 4 issue "
+                                   "slots per SM per cycle at the sampled SM clock"}
+
     ragged = bench_ragged60(jne, torch, local, args.ragged_steps) if args.ragged_steps > 0 and rank == 0 else None
     ragged_tuned = (bench_ragged60(jne, torch, local, args.ragged_steps, tune=args.tune_err)
                     if args.ragged_steps > 0 and args.tune_err > 0 and rank == 0 else None)
@@ -383,7 +399,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "gpu_launches": acc_n + fin_n,
             "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
             "ragged60": ragged, "ragged60_tuned": ragged_tuned, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
-            "cpu_baseline": cpu, "clocks": clk.summary(),
+            "cpu_baseline": cpu, "clocks": clocks,
         }))
     eng.close()
     if dist is not None:
