@@ -131,6 +131,31 @@ __device__ __forceinline__ void ff_mul(float xh, float xl, float yh, float yl, f
   e = __fmaf_rn(xl, yh, e);
 }
 
+// (hi, lo) += p + t on a pair held in shared memory: one 8-byte load and store.
+__device__ __forceinline__ void slot_acc(float2& v, float p, float t) {
+  float2 r = v;
+  ff_acc(r.x, r.y, p, t);
+  v = r;
+}
+
+// f(t) for t = lane, lane + 32, ... below N.  UNROLL: unrolled, so that the
+// lane's independent slot updates overlap instead of running one after the
+// other (7% of the time at T = 1000).  The ragged kernel, which holds every
+// dim's code, keeps the loop: unrolled, it spills registers.
+template <int N, bool UNROLL, typename F>
+__device__ __forceinline__ void for_slots(int lane, F&& f) {
+  if (UNROLL) {
+#pragma unroll
+    for (int k = 0; k < (N + 31) / 32; k++) {
+      const int t = lane + 32 * k;
+      if (t < N) f(t);
+    }
+  } else {
+#pragma unroll 1
+    for (int t = lane; t < N; t += 32) f(t);
+  }
+}
+
 // Dims up to 4 pack two runs into a warp: run A owns G rows 0..7, run B rows
 // 8..15 (walk rows 0..DIM-1, basis rows DIM..DIM+2, then zero rows), so lane g
 // holds local row g of both runs.  The three Gram blocks are then run A's G x G,
@@ -266,12 +291,12 @@ constexpr int kRecMax = JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2 + 6 * JNE_MAX_DIM + 
 struct alignas(16) WarpSmem {
   float zs[16][kZS];      // increments of the current tile: z[feature][step]
   float cm[16][kCS];      // the chunk's local Gram, staged for the merge
-  float wch[16], wcl[16];  // walk at the chunk start (float-float)
-  float tzh[16], tzl[16];  // chunk increment totals (float-float)
-  float rech[kRecMax];     // the run's record, float-float
-  float recl[kRecMax];
-  float mmh[16], mml[16];  // per feature: chunk mean m of the walk (float-float)
-  float lmh[16], lml[16];  // Lc * m
+  // float-float values are (hi, lo) pairs
+  float2 wc[16];           // walk at the chunk start
+  float2 tz[16];           // chunk increment totals
+  float2 rec[kRecMax];     // the run's record
+  float2 mm[16];           // per feature: chunk mean m of the walk
+  float2 lm[16];           // Lc * m
   float sbf[16], tzfs[16], cub[16], cuub[16], cuz[16], cuuz[16];
   unsigned short mww_pr[JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2];
 };
@@ -286,7 +311,7 @@ __device__ __forceinline__ bool lane_feature_of(int lane) {
 // One unit of a request: run `unit`, or (packed dims) runs 2 unit and
 // 2 unit + 1 -- the second only if the request has it: accumulate their moment
 // records into a.mom[slot * a.mom_ld + run].  Executed by a whole warp.
-template <int DIM, bool EXT>
+template <int DIM, bool EXT, bool UNROLL = true>
 __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, WarpSmem& sm, const jne_round_keys& rk,
                                            int lane) {
   constexpr int d = DIM;
@@ -301,16 +326,11 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
   const int nrun = min(NU, a.n_runs - run0);
   float (*zs)[kZS] = sm.zs;
   float (*cm)[kCS] = sm.cm;
-  float* wch = sm.wch;
-  float* wcl = sm.wcl;
-  float* tzh = sm.tzh;
-  float* tzl = sm.tzl;
-  float* rech = sm.rech;
-  float* recl = sm.recl;
-  float* mmh = sm.mmh;
-  float* mml = sm.mml;
-  float* lmh = sm.lmh;
-  float* lml = sm.lml;
+  float2* wc = sm.wc;
+  float2* tz = sm.tz;
+  float2* rec = sm.rec;
+  float2* mm = sm.mm;
+  float2* lm = sm.lm;
   float* sbf = sm.sbf;
   float* tzfs = sm.tzfs;
   float* cub = sm.cub;
@@ -348,12 +368,10 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
   const float invTf = 1.0f / (float)T;
   const uint32_t seed0 = a.seed_first + (uint32_t)run0;
   for (int e = lane; e < NU * NREC; e += 32) {
-    rech[e] = 0.f;
-    recl[e] = 0.f;
+    rec[e] = make_float2(0.f, 0.f);
   }
   if (lane < 16) {
-    wch[lane] = 0.f;
-    wcl[lane] = 0.f;
+    wc[lane] = make_float2(0.f, 0.f);
   }
   __syncwarp();
 
@@ -428,8 +446,15 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
       }
     }
     if (q == 0) {
-      if (g < d) two_sum(chiA, cloA, tzh[g], tzl[g]);
-      if (PAIR ? g < d : g + 8 < d) two_sum(chiB, cloB, tzh[g + 8], tzl[g + 8]);
+      float th, tl;
+      if (g < d) {
+        two_sum(chiA, cloA, th, tl);
+        tz[g] = make_float2(th, tl);
+      }
+      if (PAIR ? g < d : g + 8 < d) {
+        two_sum(chiB, cloB, th, tl);
+        tz[g + 8] = make_float2(th, tl);
+      }
     }
     __syncwarp();
     // ---- merge into the runs' records: W = m + beta (m = chunk mean of W, sum beta = 0),
@@ -456,17 +481,16 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
       // m = wc + Sb / Lc: the quotient with its exact remainder
       const float qh = __fmul_rn(Sb, ct.inv_lc);
       const float ql = __fmul_rn(__fmaf_rn(-qh, ct.lc, Sb), ct.inv_lc);
-      float mh = wch[x], ml = wcl[x];
+      const float2 w0 = wc[x];
+      float mh = w0.x, ml = w0.y;
       ff_acc(mh, ml, qh, ql);
-      mmh[x] = mh;
-      mml[x] = ml;
+      mm[x] = make_float2(mh, ml);
       float ph, pe;
       ff_mul(mh, ml, ct.lc, 0.f, ph, pe);
       float lh, ll = 0.f;
       two_sum(ph, pe, lh, ll);
-      lmh[x] = lh;
-      lml[x] = ll;
-      const float tzf = tzh[x];
+      lm[x] = make_float2(lh, ll);
+      const float tzf = tz[x].x;
       sbf[x] = Sb;
       tzfs[x] = tzf;
       cub[x] = Sub - ub * Sb;                                              // sum (u-ubar) beta
@@ -478,55 +502,63 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
     // record slots, in order: MWW | MW1 MWy MWyy | NzW | Nz1 (from wc at the end) | Nzy Nzyy.
     // One loop per slot kind, so the lanes of an iteration take one path.
     const float c1y = hf, c2y = 2.0f * ybf * hf, c2yy = hf * hf;  // y and y^2 coefficients
-    for (int t = lane; t < NU * NMWW; t += 32) {
-      const int r = t / NMWW, e = t - r * NMWW, o = 8 * r;
+    for_slots<NU * NMWW, UNROLL>(lane, [&](int t) {
+      const int r = NU == 1 ? 0 : t / NMWW, e = t - r * NMWW, o = 8 * r;
       const int p = o + (mww_pr[e] & 0xff), c = mww_pr[e] >> 8;
+      const float2 x = lm[p], y = mm[o + c];
       float ph, pe;
-      ff_mul(lmh[p], lml[p], mmh[o + c], mml[o + c], ph, pe);
-      ff_acc(rech[r * NREC + e], recl[r * NREC + e], ph,
-             __fadd_rn(pe, cm[p][c] - sbf[p] * sbf[o + c] * invLcf));
-    }
-    for (int t = lane; t < NU * NMW; t += 32) {
-      const int r = t / NMW, tt = t - r * NMW, pp = tt / d, x = 8 * r + tt - pp * d, e = r * NREC + NMWW + tt;
+      ff_mul(x.x, x.y, y.x, y.y, ph, pe);
+      slot_acc(rec[r * NREC + e], ph, __fadd_rn(pe, cm[p][c] - sbf[p] * sbf[o + c] * invLcf));
+    });
+    for_slots<NU * NMW, UNROLL>(lane, [&](int t) {
+      const int r = NU == 1 ? 0 : t / NMW, tt = t - r * NMW, pp = tt / d, x = 8 * r + tt - pp * d;
+      const int e = r * NREC + NMWW + tt;
       const float wh = pp == 0 ? 1.f : pp == 1 ? ct.ybar_hi : ct.y2bar_hi;
       const float wl = pp == 0 ? 0.f : pp == 1 ? ct.ybar_lo : ct.y2bar_lo;
       const float a1 = pp == 0 ? 0.f : pp == 1 ? c1y : c2y, a2 = pp == 2 ? c2yy : 0.f;
       float ph, pe;
-      ff_mul(wh, wl, lmh[x], lml[x], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cub[x] + a2 * cuub[x]));
-    }
-    for (int t = lane; t < NU * NNZW; t += 32) {
-      const int r = t / NNZW, tt = t - r * NNZW, za = tt / d, wb = tt - za * d, o = 8 * r;
+      const float2 v = lm[x];
+      ff_mul(wh, wl, v.x, v.y, ph, pe);
+      slot_acc(rec[e], ph, __fadd_rn(pe, a1 * cub[x] + a2 * cuub[x]));
+    });
+    for_slots<NU * NNZW, UNROLL>(lane, [&](int t) {
+      const int r = NU == 1 ? 0 : t / NNZW, tt = t - r * NNZW, za = tt / d, wb = tt - za * d, o = 8 * r;
       const int e = r * NREC + NMWW + NMW + tt;
       float ph, pe;
-      ff_mul(tzh[o + za], tzl[o + za], mmh[o + wb], mml[o + wb], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, cm[o + wb][16 + za] - tzfs[o + za] * sbf[o + wb] * invLcf));
-    }
-    for (int t = lane; t < NU * 2 * d; t += 32) {
-      const int r = t / (2 * d), tt = t - r * 2 * d, pp = tt / d, x = 8 * r + tt - pp * d;
+      const float2 x = tz[o + za], y = mm[o + wb];
+      ff_mul(x.x, x.y, y.x, y.y, ph, pe);
+      slot_acc(rec[e], ph, __fadd_rn(pe, cm[o + wb][16 + za] - tzfs[o + za] * sbf[o + wb] * invLcf));
+    });
+    for_slots<NU * 2 * d, UNROLL>(lane, [&](int t) {
+      const int r = NU == 1 ? 0 : t / (2 * d), tt = t - r * 2 * d, pp = tt / d, x = 8 * r + tt - pp * d;
       const int e = r * NREC + NMWW + NMW + NNZW + d + tt;
       const float wh = pp == 0 ? ct.ybar_hi : ct.y2bar_hi, wl = pp == 0 ? ct.ybar_lo : ct.y2bar_lo;
       const float a1 = pp == 0 ? c1y : c2y, a2 = pp == 0 ? 0.f : c2yy;
       float ph, pe;
-      ff_mul(wh, wl, tzh[x], tzl[x], ph, pe);
-      ff_acc(rech[e], recl[e], ph, __fadd_rn(pe, a1 * cuz[x] + a2 * cuuz[x]));
-    }
+      const float2 v = tz[x];
+      ff_mul(wh, wl, v.x, v.y, ph, pe);
+      slot_acc(rec[e], ph, __fadd_rn(pe, a1 * cuz[x] + a2 * cuuz[x]));
+    });
     __syncwarp();
-    if (lane_feature) ff_acc(wch[lane], wcl[lane], tzh[lane], tzl[lane]);
+    if (lane_feature) {
+      float2 w = wc[lane];
+      const float2 v = tz[lane];
+      ff_acc(w.x, w.y, v.x, v.y);
+      wc[lane] = w;
+    }
     __syncwarp();
   }
 
   // ---- write the records (slot order of jne_common.cuh) in FP64 ----
   if (lane_feature_of<DIM>(lane)) {
     const int r = PAIR ? lane >> 3 : 0, f = PAIR ? (lane & 7) : lane;
-    rech[r * NREC + jne_slot_Nz1(f, d)] = wch[lane];
-    recl[r * NREC + jne_slot_Nz1(f, d)] = wcl[lane];
+    rec[r * NREC + jne_slot_Nz1(f, d)] = wc[lane];
   }
   __syncwarp();
   const size_t ld = (size_t)a.mom_ld;
   for (int t = lane; t < NU * NREC; t += 32) {
     const int r = t / NREC, e = t - r * NREC;
-    if (r < nrun) a.mom[(size_t)e * ld + run0 + r] = (double)rech[t] + (double)recl[t];
+    if (r < nrun) a.mom[(size_t)e * ld + run0 + r] = (double)rec[t].x + (double)rec[t].y;
   }
   __syncwarp();
 }
@@ -634,18 +666,18 @@ __global__ void __launch_bounds__(kMixWarps * JNE_WARP, 4)
     const int unit = (int)(item - (unsigned long long)reqs[lo].first);
     const jne_round_keys rk = jne_make_round_keys(a.key0, a.key1);
     switch (a.dim) {
-      case 1: accum_unit<1, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 2: accum_unit<2, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 3: accum_unit<3, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 4: accum_unit<4, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 5: accum_unit<5, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 6: accum_unit<6, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 7: accum_unit<7, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 8: accum_unit<8, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 9: accum_unit<9, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 10: accum_unit<10, false>(a, unit, sm_all[wib], rk, lane); break;
-      case 11: accum_unit<11, false>(a, unit, sm_all[wib], rk, lane); break;
-      default: accum_unit<12, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 1: accum_unit<1, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 2: accum_unit<2, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 3: accum_unit<3, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 4: accum_unit<4, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 5: accum_unit<5, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 6: accum_unit<6, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 7: accum_unit<7, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 8: accum_unit<8, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 9: accum_unit<9, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 10: accum_unit<10, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      case 11: accum_unit<11, false, false>(a, unit, sm_all[wib], rk, lane); break;
+      default: accum_unit<12, false, false>(a, unit, sm_all[wib], rk, lane); break;
     }
     if (batch_done) {
       const long long first = batch_complete(batch_done, (long long)item, total, lane);
