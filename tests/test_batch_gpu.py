@@ -89,3 +89,16 @@ def test_plan_rejects_fp64_requests(engine, jne):
     with pytest.raises(jne.JneError) as ei:
         engine.plan(reqs, [o.data_ptr() for o in _outs(jne, reqs)])
     assert ei.value.code == jne.JNE_ERR_ARG
+
+
+def test_ragged_mixed_requests_equal_single_requests_bit_for_bit(engine, jne):
+    # the ragged kernel (every dim in one launch) and the single-request kernel
+    # compile the merge differently; the arithmetic per value is the same
+    reqs = [dict(model=m, dim=d, steps=t, n_runs=n, seed_first=s)
+            for m, d, t, n, s in ((0, 12, 1000, 96, 1), (4, 3, 2500, 33, 7), (1, 1, 300, 70, 3),
+                                  (3, 7, 777, 40, 11), (2, 12, 4096, 20, 5), (4, 4, 640, 65, 2))]
+    outs = _outs(jne, reqs)
+    engine.run_batch(reqs, [o.data_ptr() for o in outs])
+    engine.sync()
+    for r, o in zip(reqs, outs):
+        assert np.array_equal(o.cpu().numpy(), _single(engine, jne, r)), r
