@@ -424,7 +424,19 @@ int run_models(jne_context* ctx, const std::vector<int>& models, const std::vect
                int steps, const std::vector<uint32_t>& remaining, int precision, uint64_t base_seed) {
   const size_t nm = models.size();
   std::vector<jne_dat_writer*> w(nm, nullptr);
+  // Batches are written by a second thread while the next one computes (two
+  // buffers): the files then cost no GPU time.  The writer owns w[] while it
+  // runs; every exit path joins it first.
+  std::thread writer;
+  int wrc = 0;
+  std::string werr;
+  auto join = [&]() {
+    if (writer.joinable()) writer.join();
+    if (wrc) g_err = werr;  // the writer's message (errors are per thread)
+    return wrc;
+  };
   auto abandon = [&]() {
+    join();
     for (jne_dat_writer* x : w)
       if (x) jne_dat_abandon(x);  // keep what was written; a rerun resumes
   };
@@ -435,30 +447,42 @@ int run_models(jne_context* ctx, const std::vector<int>& models, const std::vect
       return rc;
     }
   const int64_t batch = 1 << 18;
-  std::vector<std::vector<double>> eig(nm);
+  std::vector<std::vector<double>> eig[2] = {std::vector<std::vector<double>>(nm),
+                                             std::vector<std::vector<double>>(nm)};
   std::vector<double*> outs(nm);
+  int cur = 0;
   for (size_t i = 0; i < remaining.size();) {
     // largest contiguous seed range starting at remaining[i], capped at `batch`
     size_t j = i + 1;
     while (j < remaining.size() && remaining[j] == remaining[j - 1] + 1 && (int64_t)(j - i) < batch) j++;
     const int64_t n = (int64_t)(j - i);
     for (size_t m = 0; m < nm; m++) {
-      eig[m].resize((size_t)n * jne_eigen_count(models[m], dim));
-      outs[m] = eig[m].data();
+      eig[cur][m].resize((size_t)n * jne_eigen_count(models[m], dim));
+      outs[m] = eig[cur][m].data();
     }
     rc = jne_eigs_seeded_models(ctx, models.data(), (int)nm, dim, steps, base_seed, remaining[i], n, precision,
                                 outs.data());
     if (rc) {
-      g_err = jne_last_error(ctx);
+      const std::string msg = jne_last_error(ctx);
+      abandon();
+      g_err = msg;
+      return rc;
+    }
+    if ((rc = join())) {
       abandon();
       return rc;
     }
-    for (size_t m = 0; m < nm; m++)
-      if ((rc = jne_dat_append(w[m], &remaining[i], outs[m], n, jne_eigen_count(models[m], dim)))) {
-        abandon();
-        return rc;
-      }
+    writer = std::thread([&, buf = cur, i0 = i, n]() {
+      for (size_t m = 0; m < nm && !wrc; m++)
+        if ((wrc = jne_dat_append(w[m], &remaining[i0], eig[buf][m].data(), n, jne_eigen_count(models[m], dim))))
+          werr = g_err;
+    });
+    cur ^= 1;
     i = j;
+  }
+  if ((rc = join())) {
+    abandon();
+    return rc;
   }
   for (size_t m = 0; m < nm; m++) {
     jne_dat_writer* x = w[m];
