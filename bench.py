@@ -3,8 +3,8 @@
 Workload (the headline configuration): dim 12, T = 10,000 steps, models 0-4.
 One step = one batch of R runs for each of the five models, each model a
 separate C-ABI request (seeds 1..R, counter-based Philox increments generated
-in-kernel), through the mixed-precision path (split-TF32 tensor-core Grams,
-FP32 chunks, FP64 merge and FP64 Cholesky + tridiagonal QL).
+in-kernel), through the mixed-precision path (split-FP16 tensor-core Grams,
+FP32 chunks, float-float merge and FP64 Cholesky + tridiagonal QL).
 
   value   runs/s with results left in device memory (jne_eigs_seeded_device)
   e2e     runs/s through jne_eigs_seeded: eigenvalues copied to host memory
@@ -328,13 +328,13 @@ def run_gpu(args, rank: int, world: int) -> None:
              "frac": normals_rate / rng_peak, "probe_rates": rates,
              "note": "normals/s the accumulation kernel draws vs the rate of the same Philox4x32-10 + "
                      "Box-Muller device code alone (jne_probe_rates, measured in this run)"}
-    # the tensor work the kernel executes: per 8 steps, 3 Gram blocks x 3 split products of m16n8k8 TF32
-    # (2,048 flops each); against mma.sync TF32 measured by the probe in this run
-    mma_flops = 9 * 2048 * (STEPS // 8) * R / (mean_acc_ms * 1e-3)
-    roof["tensor_pipe"] = {"executed_tflops": mma_flops / 1e12, "peak_tflops": rates["mma_tf32_flops"] / 1e12,
-                           "frac": mma_flops / rates["mma_tf32_flops"],
-                           "note": "executed split-TF32 mma.sync work (not algorithmic flops) vs the measured "
-                                   "mma.sync TF32 rate"}
+    # the tensor work the kernel executes: per 16 steps, 3 Gram blocks x 3 split products of m16n8k16 FP16
+    # (4,096 flops each); against mma.sync FP16 (FP32 accumulation) measured by the probe in this run
+    mma_flops = 9 * 4096 * (STEPS // 16) * R / (mean_acc_ms * 1e-3)
+    roof["tensor_pipe"] = {"executed_tflops": mma_flops / 1e12, "peak_tflops": rates["mma_f16_flops"] / 1e12,
+                           "frac": mma_flops / rates["mma_f16_flops"],
+                           "note": "executed split-FP16 mma.sync work (not algorithmic flops) vs the measured "
+                                   "mma.sync FP16 rate"}
 
     # SIMT issue, the kernel's binding limit: one warp instruction per cycle per scheduler
     # (4 per SM) at the SM clock sampled in the timed region
@@ -381,7 +381,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "tf32x3-split/f32/f64", "data": "synthetic (in-kernel Philox normals)",
+            "vs_baseline": None, "dtype": "f16x3-split/f32/f64", "data": "synthetic (in-kernel Philox normals)",
             "config": {"workload": f"dim {DIM}, T {STEPS}, models 0-4, {R} runs per model per step "
                                    f"(one request per model), mixed precision",
                        "runs_per_model_per_step": R, "chunk": args.chunk,

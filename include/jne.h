@@ -47,7 +47,7 @@ extern "C" {
 
 /* arithmetic of the Gram contraction */
 #define JNE_PREC_FP64 0  /* plain FP64 fused kernel */
-#define JNE_PREC_MIXED 1 /* split-TF32 tensor-core Grams, FP32 chunks, FP64 merge + solve */
+#define JNE_PREC_MIXED 1 /* split FP16/TF32 tensor-core Grams, FP32 chunks, float-float merge, FP64 solve */
 /* JNE_PREC_MIXED requests with fewer steps than this run the FP64 kernel: on
  * such short paths the FP32 chunk part is most of every moment. */
 #define JNE_MIXED_MIN_STEPS 256
@@ -71,8 +71,8 @@ void jne_close(jne_context* ctx);
 /* message of the last failed call on ctx (never null) */
 const char* jne_last_error(const jne_context* ctx);
 
-/* Steps per FP32 chunk of the mixed kernel: a multiple of 32, or 0 (the
- * default) for the largest power of two <= steps/16 in [32, 512], or
+/* Steps per FP32 chunk of the mixed kernel: a multiple of 32 up to 8192, or 0
+ * (the default) for the largest power of two <= steps/16 in [32, 512], or
  * JNE_CHUNK_TUNED for the lengths jne_autotune_chunk chose (the default rule
  * for classes it has not tuned). */
 #define JNE_CHUNK_TUNED (-1)
@@ -211,15 +211,17 @@ int jne_profile_read(jne_context* ctx, double* ms, long long* launches, int rese
 
 /* Measures, on ctx's device, the rates that bound the accumulation kernels:
  * rates[0] normals/s drawn by the kernels' own Philox4x32-10 + Box-Muller code,
- * rates[1] FP64 FMA flop/s, rates[2] TF32 mma.sync flop/s, rates[3] FP32 FMA
- * flop/s (JNE_RATE_*).  Each is one ~10-50 ms launch over 8 blocks per SM,
+ * rates[1] FP64 FMA flop/s, rates[2] TF32 mma.sync (m16n8k8) flop/s, rates[3]
+ * FP32 FMA flop/s, rates[4] FP16 mma.sync (m16n8k16, FP32 accumulation) flop/s
+ * (JNE_RATE_*).  Each is one ~10-50 ms launch over 8 blocks per SM,
  * timed with CUDA events after a warm-up launch.  Diagnostic: no counterpart in
  * the reference. */
 #define JNE_RATE_NORMALS 0
 #define JNE_RATE_DFMA 1
 #define JNE_RATE_MMA_TF32 2
 #define JNE_RATE_FFMA 3
-#define JNE_RATE_KINDS 4
+#define JNE_RATE_MMA_F16 4
+#define JNE_RATE_KINDS 5
 int jne_probe_rates(jne_context* ctx, double* rates);
 
 /* The increments the seeded path draws for these runs, scaled by sqrt(1/steps):

@@ -40,7 +40,7 @@ EXPORTS = (
     "jne_server_open", "jne_server_submit", "jne_server_wait", "jne_server_fetch", "jne_server_close",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
-RATE_KINDS = ("normals_per_s", "dfma_flops", "mma_tf32_flops", "ffma_flops")
+RATE_KINDS = ("normals_per_s", "dfma_flops", "mma_tf32_flops", "ffma_flops", "mma_f16_flops")
 
 
 class Request(ctypes.Structure):
@@ -259,7 +259,7 @@ class Engine:
 
     def probe_rates(self) -> Dict[str, float]:
         """Measured pipe rates of this GPU: normals/s of the kernels' RNG code, and
-        FP64-FMA, TF32-mma and FP32-FMA flop/s."""
+        FP64-FMA, TF32-mma, FP32-FMA and FP16-mma flop/s."""
         r = np.zeros(len(RATE_KINDS))
         self._check(self._L.jne_probe_rates(self._h, _dp(r)))
         return {k: float(r[i]) for i, k in enumerate(RATE_KINDS)}

@@ -1,5 +1,5 @@
 // jne_accum_mixed.cu -- mixed-precision fused accumulation: one warp per run,
-// the Gram contraction on the tensor cores (mma.sync m16n8k8, split TF32).
+// the Gram contraction on the tensor cores (mma.sync, hi/lo split operands).
 //
 // Same contract as the plain FP64 kernel (it replaces rng_matrix.rs:57-141,
 // johansen_statistics.rs:102-197 and the two sum_of_outer_products calls of
@@ -12,17 +12,22 @@
 // warp accumulates, in FP32 on the tensor cores, the 16 x 32 local Gram
 //     sum_tau G_tau [G_tau; z_tau]',   G = [b (d rows); 1; u; u^2; 0...],
 // with u = tau / chunk.  Each operand is split x = hi + lo with hi = x rounded
-// to the nearest TF32 value (19 bits) and every product is hi*hi + hi*lo +
-// lo*hi (three MMAs).  At the chunk end the local Gram is mapped to the global
-// moments (W = Wc + b, y = yc + h u) by the exact shift identities, summed in
-// float-float; the record is written in FP64 once per run.
+// to an 11-bit significand and every product is hi*hi + hi*lo + lo*hi (three
+// MMAs): FP16 words and m16n8k16 for the kernel's own increments, TF32 words
+// and m16n8k8 for explicit ones (see mma_split_f16).  At the chunk end the
+// local Gram is mapped to the global moments (W = Wc + b, y = yc + h u) by the
+// exact shift identities, summed in float-float; the record is written in FP64
+// once per run.
 //
-// Fragment layout (PTX ISA, mma.m16n8k8 .tf32): lane (g = lane/4, q = lane%4)
-// holds rows g and g+8 of A at k-slots q and q+4, and column g of B at the same
-// k-slots.  The sum over k does not depend on which time step a k-slot carries,
-// so slot k = q (q+4) of MMA s carries tile step 8q + 2s (8q + 2s + 1): every
-// lane owns 8 consecutive steps, which makes the scan along time cheap, and the
-// A fragment registers double as the B fragments of the G x G tiles.
+// Fragment layout (PTX ISA): lane (g = lane/4, q = lane%4) holds rows g and g+8
+// of A and column g of B, at k-slots q and q+4 (m16n8k8 .tf32) or 2q, 2q+1,
+// 2q+8, 2q+9 (m16n8k16 .f16).  The sum over k does not depend on which time
+// step a k-slot carries, so the slots of MMA s carry the lane's own steps --
+// 2s, 2s+1 (TF32) or 4s..4s+3 (FP16) of its 8 consecutive steps 8q..8q+7.
+// That makes the scan along time cheap, and the A fragment registers double as
+// the B fragments of the G x G tiles.
+#include <cuda_fp16.h>
+
 #include "jne_finalize_run.cuh"
 
 namespace {
@@ -98,6 +103,57 @@ __device__ __forceinline__ void mma_split(float (&hh)[4], float (&x)[4], const u
     mma_tf32(hh, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
 }
 
+// The same products on the FP16 split with m16n8k16 MMAs (16 steps per
+// instruction, half the MMAs of the TF32 form).  FP16 has TF32's 11-bit
+// significand, so hi * hi is exact as before, and the remainder lo is rounded to
+// nearest by the conversion instead of truncated by the tensor core.  Its range
+// is the limit (largest finite 65504, normals from 6.1e-5): it serves the
+// kernel's own increments, which are bounded -- |z| <= 5.8 by the Box-Muller
+// uniforms, so the chunk-local walk |b| <= 5.8 L <= 47,500 for chunks of at most
+// 8192 steps, and the basis rows lie in [0, 1].  Values below the normal range
+// keep an absolute error under 3e-8 through lo.  Explicit increments are
+// arbitrary and keep the TF32 split (FP32 range).
+__device__ __forceinline__ void mma_f16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                        uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void mma_f16_first(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                              uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%10,%10,%10,%10};\n"
+      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1), "f"(0.0f));
+}
+
+// The FP16 split of two consecutive steps' values of one row (an f16x2 word,
+// the first step in the low half): hi = each rounded to FP16, lo = x - hi
+// rounded to FP16.
+__device__ __forceinline__ void split_f16x2(float x0, float x1, uint32_t& h, uint32_t& l) {
+  const __half2 hh = __floats2half2_rn(x0, x1);
+  const float2 lo = sub_pair(make_float2(x0, x1), __half22float2(hh));
+  const __half2 ll = __floats2half2_rn(lo.x, lo.y);
+  h = *reinterpret_cast<const uint32_t*>(&hh);
+  l = *reinterpret_cast<const uint32_t*>(&ll);
+}
+
+template <bool FIRST>
+__device__ __forceinline__ void mma_split_f16(float (&hh)[4], float (&x)[4], const uint32_t (&ah)[4],
+                                              const uint32_t (&al)[4], uint32_t bh0, uint32_t bh1, uint32_t bl0,
+                                              uint32_t bl1) {
+  mma_f16(x, al[0], al[1], al[2], al[3], bh0, bh1);
+  mma_f16(x, ah[0], ah[1], ah[2], ah[3], bl0, bl1);
+  if (FIRST)
+    mma_f16_first(hh, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+  else
+    mma_f16(hh, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+}
+
 // Two-sum carry update: (hi, lo) += t.
 __device__ __forceinline__ void ff_add(float& hi, float& lo, float t) {
   const float s = __fadd_rn(hi, t);
@@ -171,7 +227,7 @@ struct Packing {
 // tile's increments: row f = feature f (unpacked), or row 8 r + f = feature f of
 // run r (packed); rows without a feature are zero.  See the file comment for
 // the lane <-> (row, step) mapping.
-template <int DIM, bool FULL>
+template <int DIM, bool EXT, bool FULL>
 __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, int tloc, int nvalid,
                                           float invL, const float (&cA)[4], const float (&cB)[4],
                                           float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[3][4],
@@ -256,23 +312,55 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   if (!BLOCK1)
 #pragma unroll
     for (int r = 0; r < 4; r++) hh[1][r] = 0.f;
+  if (EXT) {
+    // TF32 split, m16n8k8: MMA s carries the lane's steps 2s (k-slot q) and 2s + 1 (q + 4)
 #pragma unroll
-  for (int s = 0; s < 4; s++) {
-    const int j0 = 2 * s, j1 = 2 * s + 1;
-    // A: rows g, g + 8 at steps j0 (a0, a1) and j1 (a2, a3); block 0's B is rows g of A: (a0, a2)
-    uint32_t ah[4], al[4], b1h0, b1h1, b1l0, b1l1, b2h0, b2h1, b2l0, b2l1;
-    split_pair(make_float2(GA[j0], GB[j0]), ah[0], ah[1], al[0], al[1]);
-    split_pair(make_float2(GA[j1], GB[j1]), ah[2], ah[3], al[2], al[3]);
-    if (BLOCK1) split_pair(make_float2(BB[j0], BB[j1]), b1h0, b1h1, b1l0, b1l1);
-    split_pair(make_float2(zA[j0], zA[j1]), b2h0, b2h1, b2l0, b2l1);
-    if (s == 0) {
-      mma_split<true>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
-      if (BLOCK1) mma_split<true>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
-      mma_split<true>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
-    } else {
-      mma_split<false>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
-      if (BLOCK1) mma_split<false>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
-      mma_split<false>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+    for (int s = 0; s < 4; s++) {
+      const int j0 = 2 * s, j1 = 2 * s + 1;
+      // A: rows g, g + 8 at steps j0 (a0, a1) and j1 (a2, a3); block 0's B is rows g of A: (a0, a2)
+      uint32_t ah[4], al[4], b1h0, b1h1, b1l0, b1l1, b2h0, b2h1, b2l0, b2l1;
+      split_pair(make_float2(GA[j0], GB[j0]), ah[0], ah[1], al[0], al[1]);
+      split_pair(make_float2(GA[j1], GB[j1]), ah[2], ah[3], al[2], al[3]);
+      if (BLOCK1) split_pair(make_float2(BB[j0], BB[j1]), b1h0, b1h1, b1l0, b1l1);
+      split_pair(make_float2(zA[j0], zA[j1]), b2h0, b2h1, b2l0, b2l1);
+      if (s == 0) {
+        mma_split<true>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
+        if (BLOCK1) mma_split<true>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
+        mma_split<true>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+      } else {
+        mma_split<false>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
+        if (BLOCK1) mma_split<false>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
+        mma_split<false>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+      }
+    }
+  } else {
+    // FP16 split, m16n8k16: MMA s carries the lane's steps 4s, 4s + 1 (k-slots 2q, 2q + 1) and
+    // 4s + 2, 4s + 3 (2q + 8, 2q + 9)
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const int j = 4 * s;
+      // A words: row g at steps j, j+1; row g+8 at j, j+1; row g at j+2, j+3; row g+8 at j+2, j+3.
+      // Block 0's B is rows g of A: words 0 and 2.
+      uint32_t ah[4], al[4], b1h0, b1h1, b1l0, b1l1, b2h0, b2h1, b2l0, b2l1;
+      split_f16x2(GA[j], GA[j + 1], ah[0], al[0]);
+      split_f16x2(GB[j], GB[j + 1], ah[1], al[1]);
+      split_f16x2(GA[j + 2], GA[j + 3], ah[2], al[2]);
+      split_f16x2(GB[j + 2], GB[j + 3], ah[3], al[3]);
+      if (BLOCK1) {
+        split_f16x2(BB[j], BB[j + 1], b1h0, b1l0);
+        split_f16x2(BB[j + 2], BB[j + 3], b1h1, b1l1);
+      }
+      split_f16x2(zA[j], zA[j + 1], b2h0, b2l0);
+      split_f16x2(zA[j + 2], zA[j + 3], b2h1, b2l1);
+      if (s == 0) {
+        mma_split_f16<true>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
+        if (BLOCK1) mma_split_f16<true>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
+        mma_split_f16<true>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+      } else {
+        mma_split_f16<false>(hh[0], accx[0], ah, al, ah[0], ah[2], al[0], al[2]);
+        if (BLOCK1) mma_split_f16<false>(hh[1], accx[1], ah, al, b1h0, b1h1, b1l0, b1l1);
+        mma_split_f16<false>(hh[2], accx[2], ah, al, b2h0, b2h1, b2l0, b2l1);
+      }
     }
   }
   // empty the tile's hi*hi accumulator into the chunk sum (round to nearest)
@@ -417,9 +505,9 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
       const int nvalid = min(32, T - t0);
       const int tloc = t0 - c0 + 8 * q;
       if (nvalid == 32)
-        tile_body<DIM, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
+        tile_body<DIM, EXT, true>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
       else
-        tile_body<DIM, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
+        tile_body<DIM, EXT, false>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
       __syncwarp();
     }
 

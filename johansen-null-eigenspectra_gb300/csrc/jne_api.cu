@@ -91,8 +91,9 @@ const char* jne_last_error(const jne_context* c) { return c ? c->err.c_str() : k
 
 int jne_set_chunk(jne_context* c, int chunk) {
   if (!c) return JNE_ERR_ARG;
-  if (chunk != 0 && chunk != JNE_CHUNK_TUNED && (chunk < 32 || chunk % 32 != 0 || chunk > (1 << 20)))
-    return fail(c, JNE_ERR_ARG, "chunk must be 0 (adaptive), JNE_CHUNK_TUNED or a multiple of 32");
+  // at most 8192 steps: the FP16 operands of the mixed kernel then hold any chunk-local walk
+  if (chunk != 0 && chunk != JNE_CHUNK_TUNED && (chunk < 32 || chunk % 32 != 0 || chunk > 8192))
+    return fail(c, JNE_ERR_ARG, "chunk must be 0 (adaptive), JNE_CHUNK_TUNED or a multiple of 32 up to 8192");
   c->chunk = chunk;
   return JNE_OK;
 }

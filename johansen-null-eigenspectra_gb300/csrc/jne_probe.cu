@@ -2,8 +2,9 @@
 // measured on the running GPU with the same device code the kernels use.
 //   rates[0]  normals/s  drawn by jne_normal_quad (Philox4x32-10 + Box-Muller)
 //   rates[1]  FP64 flop/s of independent DFMA chains
-//   rates[2]  flop/s of mma.sync.m16n8k8 TF32 (the mixed kernel's instruction)
+//   rates[2]  flop/s of mma.sync.m16n8k8 TF32 (the mixed kernel's form for explicit increments)
 //   rates[3]  FP32 flop/s of independent FFMA chains
+//   rates[4]  flop/s of mma.sync.m16n8k16 FP16 with FP32 accumulation (the form for its own increments)
 #include "jne_context.h"
 
 using namespace jne_detail;
@@ -70,6 +71,27 @@ __global__ void k_probe_mma(float* out, int iters) {
   out[tid] = s;
 }
 
+__global__ void k_probe_mma_f16(float* out, int iters) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t a0 = 0x3c003c00u ^ (tid & 0x100u), b0 = 0x3c003c00u;  // f16x2 words near 1.0
+  float c[8][4];
+  for (int j = 0; j < 8; j++)
+    for (int q = 0; q < 4; q++) c[j][q] = 0.f;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+          "{%0,%1,%2,%3};\n"
+          : "+f"(c[j][0]), "+f"(c[j][1]), "+f"(c[j][2]), "+f"(c[j][3])
+          : "r"(a0), "r"(a0), "r"(a0), "r"(a0), "r"(b0), "r"(b0));
+  }
+  float s = 0;
+  for (int j = 0; j < 8; j++)
+    for (int q = 0; q < 4; q++) s += c[j][q];
+  out[tid] = s;
+}
+
 }  // namespace
 
 extern "C" int jne_probe_rates(jne_context* c, double* rates) {
@@ -106,6 +128,8 @@ extern "C" int jne_probe_rates(jne_context* c, double* rates) {
                    8.0 * 16 * 8 * 8 * 2 * it_m * n / 32.0);
   rates[3] = timed([&](int w) { k_probe_ffma<<<blocks, kProbeThreads, 0, st>>>((float*)buf, w ? w : it_f); },
                    32.0 * it_f * n);
+  rates[4] = timed([&](int w) { k_probe_mma_f16<<<blocks, kProbeThreads, 0, st>>>((float*)buf, w ? w : it_m); },
+                   8.0 * 16 * 8 * 16 * 2 * it_m * n / 32.0);
   cudaError_t e = cudaGetLastError();
   cudaEventDestroy(a);
   cudaEventDestroy(b);

@@ -209,7 +209,8 @@ def test_distribution_matches_cpu_oracle(engine, oracle):
 
 def test_probe_rates_are_measured(engine):
     r = engine.probe_rates()
-    assert set(r) == {"normals_per_s", "dfma_flops", "mma_tf32_flops", "ffma_flops"}
+    assert set(r) == {"normals_per_s", "dfma_flops", "mma_tf32_flops", "ffma_flops", "mma_f16_flops"}
     assert 1e10 < r["normals_per_s"] < 1e14
     assert 1e11 < r["dfma_flops"] < r["ffma_flops"]
     assert 1e12 < r["mma_tf32_flops"] < 1e16
+    assert 1e12 < r["mma_f16_flops"] < 1e16
