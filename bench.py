@@ -39,13 +39,13 @@ UNIT = "runs/s"
 
 # DRAM bytes (read + write) of one k_accum_mixed<12> launch (accumulation + fused
 # finalize) per run, from an ncu capture of the full 200,000-run launch
-# (profiles/k_accum_mixed_dim12_T10k_dram.md): 27,378,432 B read + 951,754,752 B written.
+# (profiles/k_accum_mixed_dim12_T10k_dram.md): 24,073,472 B read + 965,540,864 B written.
 # Algorithmic: 2,352 B of record written and read back, 96 B of eigenvalues per run.
-ACCUM_DRAM_BYTES_PER_RUN = (27_378_432 + 951_754_752) / 200_000
+ACCUM_DRAM_BYTES_PER_RUN = (24_073_472 + 965_540_864) / 200_000
 # Warp instructions k_accum_mixed<12> issues per run at T = 10,000 (accumulation plus
 # the run's share of its fused finalize batch), from an ncu capture of an 8,192-run
 # launch (profiles/k_accum_mixed_dim12_T10k_8192runs_full.md).
-ACCUM_WARP_INST_PER_RUN = 175_475
+ACCUM_WARP_INST_PER_RUN = 174_587
 
 
 def k_of(model: int) -> int:
