@@ -16,7 +16,6 @@
 #include <cstring>
 #include <string>
 #include <thread>
-#include <unordered_set>
 #include <vector>
 
 #include "../../include/jne.h"
@@ -391,7 +390,7 @@ int remaining_seeds(const std::string& dir, int model, int dim, int steps, int64
   int rc = jne_simulation_filename(dir.c_str(), model, dim, steps, buf, sizeof buf);
   if (rc) return rc;
   *path = buf;
-  std::unordered_set<uint32_t> done;
+  std::vector<uint32_t> done;  // seeds already in the file, sorted
   if (file_exists(buf)) {
     std::vector<unsigned char> b;
     Parsed p;
@@ -400,13 +399,20 @@ int remaining_seeds(const std::string& dir, int model, int dim, int steps, int64
         if (!quiet) std::printf("WARNING: Existing file has incompatible parameters; recreating %s\n", buf);
         std::remove(buf);
       } else {
-        done.insert(p.seeds.begin(), p.seeds.end());
+        done = std::move(p.seeds);
+        std::sort(done.begin(), done.end());
       }
     }
   }
+  // seeds 1..num_runs not in the file, by one merge walk over the sorted seeds
   remaining->clear();
-  for (int64_t s = 1; s <= num_runs; s++)
-    if (!done.count((uint32_t)s)) remaining->push_back((uint32_t)s);
+  remaining->reserve((size_t)num_runs);
+  size_t d = 0;
+  for (int64_t s = 1; s <= num_runs; s++) {
+    while (d < done.size() && done[d] < (uint32_t)s) d++;
+    if (d < done.size() && done[d] == (uint32_t)s) continue;
+    remaining->push_back((uint32_t)s);
+  }
   if (!quiet) {
     if (remaining->empty())
       std::printf("SUCCESS: calculation for this model already completed, skipping\n");
