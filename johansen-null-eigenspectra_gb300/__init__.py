@@ -224,7 +224,7 @@ class Engine:
             raise JneError(rc, self._L.jne_last_error(self._h).decode(errors="replace"))
 
     def set_chunk(self, chunk: int) -> None:
-        """Steps per FP32 chunk of the mixed kernel: 0 (default rule), CHUNK_TUNED or a multiple of 32."""
+        """Steps per FP32 chunk of the mixed kernel: 0 (default rule), CHUNK_TUNED or a multiple of 32 up to 8192."""
         self._check(self._L.jne_set_chunk(self._h, chunk))
 
     def autotune_chunk(self, dim: int, steps: int, max_rel_err: float = 5e-7, sample_runs: int = 512) -> Tuple[int, float]:

@@ -158,6 +158,12 @@ def test_bad_arguments(engine, jne):
     with pytest.raises(jne.JneError) as ei:
         engine.set_chunk(100)
     assert ei.value.code == jne.JNE_ERR_ARG
+    # chunks longer than 8192 steps could push the chunk-local walk past FP16's range
+    with pytest.raises(jne.JneError) as ei:
+        engine.set_chunk(8192 + 32)
+    assert ei.value.code == jne.JNE_ERR_ARG
+    engine.set_chunk(8192)
+    engine.set_chunk(0)
 
 
 def test_budget_is_enforced(jne):
