@@ -220,3 +220,14 @@ def test_probe_rates_are_measured(engine):
     assert 1e11 < r["dfma_flops"] < r["ffma_flops"]
     assert 1e12 < r["mma_tf32_flops"] < 1e16
     assert 1e12 < r["mma_f16_flops"] < 1e16
+
+
+def test_longest_chunk_keeps_fp16_operands_finite(jne):
+    # chunks of 8192 steps: the chunk-local walk is the largest FP16 operand; results stay finite and close
+    # to FP64 (long chunks only cost accuracy, here of order 1e-5)
+    with jne.Engine(0, chunk=8192) as eng:
+        for dim in (1, 12):
+            m = eng.eigs_seeded(0, dim, 16384, 1, 64, precision=1)
+            f = eng.eigs_seeded(0, dim, 16384, 1, 64, precision=0)
+            assert np.all(np.isfinite(m))
+            assert normwise_err(m, f, 1.0) < 1e-3, dim
