@@ -81,9 +81,13 @@ uint64_t get_u64(const unsigned char* p) {
   return v;
 }
 void put_f64(unsigned char* p, double x) {
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+  std::memcpy(p, &x, 8);  // the file's byte order is the host's
+#else
   uint64_t u;
   std::memcpy(&u, &x, 8);
   put_u64(p, u);
+#endif
 }
 double get_f64(const unsigned char* p) {
   const uint64_t u = get_u64(p);
@@ -316,14 +320,44 @@ int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs,
                                         ", actual " + std::to_string(k) + " (model " + std::to_string(w->model) +
                                         ", dim " + std::to_string(w->dim) + ", steps " + std::to_string(w->steps) +
                                         ")");
-  w->rec.resize(5 + 1 + 8 * (size_t)k);
-  for (int64_t r = 0; r < n; r++) {
-    size_t len = uleb_encode(seeds[r], w->rec.data());
-    w->rec[len++] = (unsigned char)k;
-    for (int j = 0; j < k; j++) put_f64(&w->rec[len + 8 * j], eigs[(size_t)r * k + j]);
-    len += 8 * (size_t)k;
-    if (std::fwrite(w->rec.data(), 1, len, w->f) != len) return dat_fail(JNE_ERR_IO, "record write failed");
-    w->count++;
+  // Records are encoded into one block and written with one call per block;
+  // large batches are encoded by several threads, each into its own byte
+  // range (record sizes differ only in the seed's ULEB128 length).
+  const size_t fixed = 1 + 8 * (size_t)k;
+  auto rec_size = [&](uint32_t seed) {
+    return fixed + 1 + (seed >= (1u << 7)) + (seed >= (1u << 14)) + (seed >= (1u << 21)) + (seed >= (1u << 28));
+  };
+  auto encode = [&](int64_t r0, int64_t r1, unsigned char* out) {
+    for (int64_t r = r0; r < r1; r++) {
+      size_t len = uleb_encode(seeds[r], out);
+      out[len++] = (unsigned char)k;
+      for (int j = 0; j < k; j++) put_f64(out + len + 8 * j, eigs[(size_t)r * k + j]);
+      out += len + 8 * (size_t)k;
+    }
+  };
+  const int64_t block = 1 << 20;  // records per block
+  for (int64_t b0 = 0; b0 < n; b0 += block) {
+    const int64_t b1 = std::min(n, b0 + block);
+    const int parts = (b1 - b0) >= (1 << 16) ? (int)std::min<unsigned>(8, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    std::vector<size_t> off((size_t)parts + 1, 0);
+    auto part_lo = [&](int p) { return b0 + (b1 - b0) * p / parts; };
+    for (int p = 0; p < parts; p++) {
+      size_t bytes = 0;
+      for (int64_t r = part_lo(p); r < part_lo(p + 1); r++) bytes += rec_size(seeds[r]);
+      off[(size_t)p + 1] = off[(size_t)p] + bytes;
+    }
+    w->rec.resize(off[(size_t)parts]);
+    if (parts == 1) {
+      encode(b0, b1, w->rec.data());
+    } else {
+      std::vector<std::thread> th;
+      for (int p = 0; p < parts; p++)
+        th.emplace_back([&, p]() { encode(part_lo(p), part_lo(p + 1), w->rec.data() + off[(size_t)p]); });
+      for (std::thread& t : th) t.join();
+    }
+    if (std::fwrite(w->rec.data(), 1, w->rec.size(), w->f) != w->rec.size())
+      return dat_fail(JNE_ERR_IO, "record write failed");
+    w->count += b1 - b0;
   }
   return JNE_OK;
 }
