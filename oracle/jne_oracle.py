@@ -69,10 +69,16 @@ def philox_words(base_seed: int, dim: int, run_seed: int, steps: int) -> np.ndar
 
 def normals(base_seed: int, dim: int, run_seed: int, steps: int) -> np.ndarray:
     """Standard normals of one run, shape (steps, dim) (Box-Muller in float64)."""
-    w = philox_words(base_seed, dim, run_seed, steps).astype(np.float64)
-    u = (np.floor(w / 512.0) + 0.5) / 8388608.0  # top 23 bits + half an ulp
-    r01 = np.sqrt(-2.0 * np.log(u[..., 0]))
-    r23 = np.sqrt(-2.0 * np.log(u[..., 2]))
+    words = philox_words(base_seed, dim, run_seed, steps)
+    w = words.astype(np.float64)
+    u = (np.floor(w / 512.0) + 0.5) / 8388608.0  # angle words: top 23 bits + half an ulp
+    # radius words: leading 24 bits (rounded toward zero to a float), + 1/2, times 2^-32, rounded to a float
+    nb = np.where(words > 0, np.floor(np.log2(np.maximum(w, 1.0))).astype(np.int64) + 1, 0)
+    drop = np.maximum(nb - 24, 0).astype(np.uint64)
+    t = ((words.astype(np.uint64) >> drop) << drop).astype(np.float64)
+    ur = ((t + 0.5) / 4294967296.0).astype(np.float32).astype(np.float64)
+    r01 = np.sqrt(-2.0 * np.log(ur[..., 0]))
+    r23 = np.sqrt(-2.0 * np.log(ur[..., 2]))
     t01 = 2.0 * np.pi * u[..., 1] - np.pi
     t23 = 2.0 * np.pi * u[..., 3] - np.pi
     z = np.stack([r01 * np.cos(t01), r01 * np.sin(t01), r23 * np.cos(t23), r23 * np.sin(t23)], axis=2)
@@ -279,6 +285,10 @@ def lib() -> ctypes.CDLL:
         L.jno_eigs_from_increments.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, dp]
         L.jno_eigs_seeded.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.c_uint32, ctypes.c_int, ctypes.c_int, dp]
+        L.jno_eigs_seeded_xoshiro.argtypes = L.jno_eigs_seeded.argtypes
+        L.jno_eigs_from_increments_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int,
+                                                  ctypes.c_int, dp]
+        L.jno_xoshiro_normals.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, dp]
         _lib = L
     return _lib
 
@@ -323,13 +333,36 @@ def c_sum_of_outer_products(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     return out
 
 
-def c_eigs_from_increments(model: int, dB: np.ndarray) -> np.ndarray:
-    """dB: (n_runs, steps, dim) array (each run's dim x T column-major matrix); returns (n_runs, k)."""
+def c_eigs_from_increments(model: int, dB: np.ndarray, n_threads: int = 1) -> np.ndarray:
+    """dB: (n_runs, steps, dim) array (each run's dim x T column-major matrix); returns (n_runs, k).
+    n_threads > 1 splits the runs over POSIX threads (same results)."""
     dB = np.ascontiguousarray(dB, dtype=np.float64)
     n, steps, dim = dB.shape
     k = eigen_count(model, dim)
     out = np.zeros((n, k))
-    rc = lib().jno_eigs_from_increments(model, dim, steps, _dp(dB), n, _dp(out))
+    if n_threads > 1:
+        rc = lib().jno_eigs_from_increments_mt(model, dim, steps, _dp(dB), n, n_threads, _dp(out))
+    else:
+        rc = lib().jno_eigs_from_increments(model, dim, steps, _dp(dB), n, _dp(out))
+    if rc < 0:
+        raise ValueError("bad arguments")
+    return out
+
+
+def c_xoshiro_normals(base_seed: int, run_seed: int, n: int) -> np.ndarray:
+    """n standard normals of the independent xoshiro256++ / Box-Muller stream (53-bit uniforms)."""
+    out = np.zeros(n)
+    lib().jno_xoshiro_normals(base_seed, run_seed, n, _dp(out))
+    return out
+
+
+def c_eigs_seeded_xoshiro(model: int, dim: int, steps: int, seed_first: int, n_runs: int,
+                          n_threads: int = 1, base_seed: int = DEFAULT_BASE_SEED) -> np.ndarray:
+    """Runs of the dense algorithm on increments from the independent xoshiro256++ stream: a sample of
+    the same null distribution that shares no random number with the kernels (distribution tests)."""
+    k = eigen_count(model, dim)
+    out = np.zeros((n_runs, k))
+    rc = lib().jno_eigs_seeded_xoshiro(model, dim, steps, base_seed, seed_first, n_runs, n_threads, _dp(out))
     if rc < 0:
         raise ValueError("bad arguments")
     return out

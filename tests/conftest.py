@@ -34,7 +34,7 @@ def oracle():
 
 @pytest.fixture(scope="session")
 def golden():
-    from gen_golden import load_increments
+    from gen_golden import generated_increments, load_increments
 
     data = np.load(os.path.join(ROOT, "tests", "golden", "golden_eigs.npz"))
     cases = {}
@@ -42,9 +42,14 @@ def golden():
         if key.startswith("z_"):
             _, d, t = key.split("_")
             cases[(int(d[1:]), int(t[1:]))] = load_increments(data[key])
+        elif key.startswith("gseed_"):  # stored as (runs, seed): increments regenerated
+            _, d, t = key.split("_")
+            dim, steps = int(d[1:]), int(t[1:])
+            runs, seed = (int(x) for x in data[key])
+            cases[(dim, steps)] = generated_increments(dim, steps, runs, seed)
     eigs = {}
     for key in data.files:
-        if key.startswith("eig_"):
+        if key.startswith("eig_") or key.startswith("geig_"):
             _, m, d, t = key.split("_")
             eigs[(int(m[1:]), int(d[1:]), int(t[1:]))] = data[key]
     return cases, eigs

@@ -98,6 +98,41 @@ def test_golden_fixture_is_the_dggev_twin(oracle, golden):
         assert normwise_err(got, ref) < 1e-12
 
 
+def test_golden_fixture_covers_the_benchmarked_shape(golden):
+    cases, eigs = golden
+    assert cases[(12, 10_000)].shape == (4, 10_000, 12)
+    assert all((m, 12, 10_000) in eigs for m in range(5))
+
+
+def test_threaded_increments_entry_agrees(oracle):
+    dB = np.random.default_rng(11).standard_normal((9, 257, 5)) / np.sqrt(257)
+    for model in (0, 3):
+        assert np.array_equal(oracle.c_eigs_from_increments(model, dB),
+                              oracle.c_eigs_from_increments(model, dB, n_threads=4))
+
+
+def test_independent_stream_is_standard_normal_and_untruncated(oracle):
+    """xoshiro256++ + Box-Muller on 53-bit uniforms: moments, a KS test, the 4-sigma tail mass
+    (6.33e-5), independence across run seeds, and the same draws in the seeded batch."""
+    from scipy.stats import kstest, norm
+
+    z = oracle.c_xoshiro_normals(oracle.DEFAULT_BASE_SEED, 5, 2_000_000)
+    assert abs(z.mean()) < 5 * np.sqrt(1 / z.size) and abs(z.var() - 1) < 5 * np.sqrt(2 / z.size)
+    assert kstest(z, "norm").pvalue > 1e-3
+    tail = np.mean(np.abs(z) > 4.0)
+    p4 = 2 * norm.sf(4.0)
+    assert abs(tail - p4) < 5 * np.sqrt(p4 / z.size)
+    other = oracle.c_xoshiro_normals(oracle.DEFAULT_BASE_SEED, 6, 100_000)
+    assert abs(np.corrcoef(z[:100_000], other)[0, 1]) < 0.02
+    assert not np.array_equal(z[:10], oracle.c_xoshiro_normals(oracle.DEFAULT_BASE_SEED + 1, 5, 10))
+    # the seeded batch walks exactly these draws (time-major, scaled by sqrt(dt))
+    zz = oracle.c_xoshiro_normals(oracle.DEFAULT_BASE_SEED, 3, 3 * 200).reshape(200, 3) / np.sqrt(200)
+    one = oracle.c_eigs_seeded_xoshiro(4, 3, 200, 3, 1)[0]
+    assert normwise_err(oracle.eigs_dense(4, zz.T), one) < 1e-10
+    many = oracle.c_eigs_seeded_xoshiro(4, 3, 200, 1, 7, n_threads=3)
+    assert np.array_equal(many[2], one)
+
+
 def test_eigen_counts(oracle):
     # basic_api.rs:35 (dim for model 0), thread_manager.rs:40-44 (dim+1 for models 1 and 3)
     assert [oracle.eigen_count(m, 2) for m in range(5)] == [2, 3, 2, 3, 2]
