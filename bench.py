@@ -363,7 +363,13 @@ def run_gpu(args, rank: int, world: int) -> None:
                 "workload": f"models 0-4 x {R} seeds, dim {DIM}, T {STEPS}, mixed, one accumulation per seed "
                             "(jne_eigs_seeded_models), eigenvalues copied to host memory; wall clock",
                 "note": "not the headline: the headline runs one request per model, as the reference does"}
-    serving = bench_serving(jne, local, args.serve_seconds) if args.serve_seconds > 0 and rank == 0 else None
+    serving = None
+    if rank == 0 and (args.serve_seconds > 0 or args.serve_low_seconds > 0):
+        serving = {}
+        if args.serve_low_seconds > 0:
+            serving["low"] = bench_serving(jne, local, args.serve_low_seconds, rate=args.serve_low_rate)
+        if args.serve_seconds > 0:
+            serving["high"] = bench_serving(jne, local, args.serve_seconds, rate=args.serve_rate)
 
     cpu = None
     if rank == 0 and args.cpu_runs != 0:
@@ -376,6 +382,10 @@ def run_gpu(args, rank: int, world: int) -> None:
             v, per, dt = cpu_sample_for(oracle, args.cpu_seconds, threads, 16 * threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{per} runs x 5 models (seeds 1..{per}), dim {DIM}, T {STEPS}, {dt:.1f} s wall"}
+        if precision is not None and args.oracle_runs > 0:
+            # the oracle as the checker of the precision line: its dense restatement on the increments the
+            # kernels draw for the first runs, against the mixed and FP64 results of the same seeds
+            precision["vs_oracle"] = precision_vs_oracle(jne, local, oracle, args.oracle_runs, threads)
 
     if rank == 0:
         print(json.dumps({
@@ -493,9 +503,29 @@ def bench_precision(jne, torch, local: int, runs: int, subset: int = 10_000) -> 
                         f"{ns} vs the plain FP64 kernel on the same seeds"}
 
 
+def precision_vs_oracle(jne, local: int, oracle, runs: int, threads: int) -> dict:
+    """Model 4, dim 12, T 1e4, seeds 1..runs: max-eig / trace error of the mixed kernel and the normwise error
+    of the FP64 kernel against the CPU oracle walking the same increments (exported by the kernels' RNG)."""
+    with jne.Engine(local) as eng:
+        dB, _ = eng.export_increments(DIM, STEPS, 1, runs)
+        mix = eng.eigs_seeded(4, DIM, STEPS, 1, runs, precision=jne.PREC_MIXED)
+        f64 = eng.eigs_seeded(4, DIM, STEPS, 1, runs, precision=jne.PREC_FP64)
+    ref = oracle.c_eigs_from_increments(4, dB, n_threads=threads)
+    rel_max = np.abs(mix[:, 0] - ref[:, 0]) / ref[:, 0]
+    rel_tr = np.abs(mix.sum(1) - ref.sum(1)) / ref.sum(1)
+    nw = np.max(np.abs(f64 - ref), axis=1) / np.max(np.abs(ref), axis=1)
+    return {"runs": runs, "mixed_maxeig_rel_err_max": float(rel_max.max()),
+            "mixed_trace_rel_err_max": float(rel_tr.max()), "fp64_normwise_err_max": float(nw.max()),
+            "oracle": "C restatement of the dense reference algorithm on the kernels' own increments"}
+
+
 def bench_serving(jne, local: int, seconds: float, rate: float = 200.0, seed: int = 0xC5) -> dict:
     """Poisson arrivals (mean `rate` req/s) for `seconds`; model U{0..4}, dim U{1..12}, T log-U[500, 2e4],
-    runs log-U[1e3, 1e6], per-request seed; 40 GB budget; latency = finish - submit."""
+    runs log-U[1e3, 1e6], per-request seed; 40 GB budget.  Latency = finish - submit, split into queueing
+    (start - submit: waiting for admission and the first iteration) and service (finish - start).  Offered
+    load = runs submitted / arrival window; served = runs / makespan (first submit to last finish).  When the
+    offered load exceeds what the GPU serves, the backlog grows for the whole window and the latency measures
+    how long it takes to drain, not a steady state: the line says so (`saturated`)."""
     rng = np.random.default_rng(seed)
     arrivals, t = [], 0.0
     while True:
@@ -525,13 +555,30 @@ def bench_serving(jne, local: int, seconds: float, rate: float = 200.0, seed: in
             for i in ids:
                 srv.fetch(i)
     lat = np.array([done[i].finish_s - done[i].submit_s for i in ids])
+    queue = np.array([done[i].start_s - done[i].submit_s for i in ids])
+    service = np.array([done[i].finish_s - done[i].start_s for i in ids])
     span = max(c.finish_s for c in done.values()) - min(c.submit_s for c in done.values())
+    window = max(at for at, _ in arrivals) if arrivals else seconds
     ok = sum(1 for c in done.values() if c.status == jne.JNE_OK)
+    offered, served = total_runs / max(window, 1e-9), total_runs / span
+    # below saturation the server keeps up: the last request finishes soon after the last arrival; above
+    # it a backlog builds and drains after the window
+    saturated = bool(span > 1.2 * window + 0.5)
+
+    def pct(x):
+        return {"p50": float(np.percentile(x, 50)), "p99": float(np.percentile(x, 99))}
+
     return {"requests": len(ids), "ok": ok, "offered_req_per_s": rate, "arrival_seconds": seconds,
-            "total_runs": total_runs, "runs_per_s": total_runs / span, "p50_latency_s": float(np.percentile(lat, 50)),
-            "p99_latency_s": float(np.percentile(lat, 99)), "makespan_s": span,
-            "workload": "Poisson 200 req/s; model U{0..4}, dim U{1..12}, T log-U[500,2e4], runs log-U[1e3,1e6], "
-                        "per-request seed; continuous batching, 40 GB budget, mixed precision"}
+            "total_runs": total_runs, "offered_runs_per_s": offered, "served_runs_per_s": served,
+            "runs_per_s": served, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "queue_s": pct(queue), "service_s": pct(service),
+            "makespan_s": span, "saturated": saturated,
+            "note": ("offered load above the served rate: the backlog grows through the arrival window and the "
+                     "latencies measure its drain" if saturated else
+                     "offered load below the served rate: steady-state latencies"),
+            "workload": f"Poisson {rate:g} req/s for {seconds:g} s; model U{{0..4}}, dim U{{1..12}}, "
+                        "T log-U[500,2e4], runs log-U[1e3,1e6], per-request seed; continuous batching, "
+                        "40 GB budget, mixed precision"}
 
 
 def main() -> None:
@@ -549,9 +596,16 @@ def main() -> None:
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per accumulation launch (default: the committed capture, scaled by runs)")
     ap.add_argument("--ragged-steps", type=int, default=2, help="timed replays of the ragged 60-pair plan (0: skip)")
-    ap.add_argument("--serve-seconds", type=float, default=1.0, help="Poisson arrival window of the serving run (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=3.0,
+                    help="arrival window of the serving run at --serve-rate (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals per second (saturating)")
+    ap.add_argument("--serve-low-seconds", type=float, default=20.0,
+                    help="arrival window of the serving run at --serve-low-rate (0: skip)")
+    ap.add_argument("--serve-low-rate", type=float, default=50.0, help="Poisson arrivals per second (below saturation)")
     ap.add_argument("--tune-err", type=float, default=1e-6,
                     help="error bound of the chunk autotuner for the tuned ragged line (0: skip)")
+    ap.add_argument("--oracle-runs", type=int, default=200,
+                    help="runs of the model-4 precision line also checked against the CPU oracle (0: skip)")
     ap.add_argument("--c3-runs", type=int, default=10_000_000,
                     help="model-4 precision run: mixed runs (error on the first 10,000 vs FP64; 0: skip)")
     ap.add_argument("--rng-peak", type=float, default=None,

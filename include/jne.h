@@ -124,24 +124,27 @@ int jne_eigs_seeded_models(jne_context* ctx, const int* models, int n_models, in
 
 /* No counterpart in the reference crate.  The seeded batch for callers that
  * cannot allocate device memory -- a host framework that owns the GPU's
- * allocator, a region being captured into a CUDA graph, a real-time loop that
- * allows no allocation after start-up.  It needs no context: its scratch (the
- * moment records and small tables) is one file-scope __device__ array of
- * JNE_NOALLOC_SCRATCH_BYTES (4.7 MiB) that every GPU loading this library
- * holds until the process exits, and it calls no cudaMalloc, cudaFree or
- * allocating library routine.  Results go to out_device (n_runs x k doubles)
- * on `stream` (a cudaStream_t; null = the legacy default stream); the call
- * waits for them.  At most JNE_NOALLOC_MAX_RUNS runs per call (and, for mixed
- * precision, at most JNE_NOALLOC_MAX_CHUNKS chunks: 2,097,152 steps), else
- * JNE_ERR_BUDGET.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the one array, so calls
- * whose GPU work overlaps (other threads or streams) race and must be
- * serialised by the caller.  The message of a failed call comes from
+ * allocator and forbids foreign allocations, a real-time loop that allows no
+ * allocation after start-up.  It needs no context: its scratch (the moment
+ * records, the chunk and entry tables, the counters and the status word) is one
+ * file-scope __device__ array of JNE_NOALLOC_SCRATCH_BYTES (4.7 MiB) that every
+ * GPU loading this library holds until the process exits, and it calls no
+ * cudaMalloc, cudaFree or allocating library routine.  It runs the kernels and
+ * tables of jne_eigs_seeded, so the results are the same bits.  Results go to
+ * out_device (n_runs x k doubles) on `stream` (a cudaStream_t; null = the
+ * legacy default stream); the call waits for them (it reads the status word
+ * back and synchronizes the stream).  At most JNE_NOALLOC_MAX_RUNS runs per call
+ * (and, for mixed precision, at most JNE_NOALLOC_MAX_CHUNKS chunks: 2,097,152
+ * steps), else JNE_ERR_BUDGET.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the one array, which
+ * keeps the last call's contents (each call clears the words that must start at
+ * zero), so calls whose GPU work overlaps (other threads or streams) race and
+ * must be serialised by the caller.  The message of a failed call comes from
  * jne_noalloc_last_error (per thread). */
 #define JNE_NOALLOC_MAX_RUNS 2048
 #define JNE_NOALLOC_MAX_CHUNKS 4096
-#define JNE_NOALLOC_SCRATCH_BYTES 4956416
+#define JNE_NOALLOC_SCRATCH_BYTES 4956672
 int jne_eigs_seeded_noalloc(int device, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
                             int n_runs, int precision, double* out_device, void* stream);
 const char* jne_noalloc_last_error(void);
@@ -159,6 +162,17 @@ typedef struct jne_request {
  * src/main.rs:85-136, is one batch).  outs_device[i] receives request i's
  * n_runs x k values.  Asynchronous, like jne_eigs_seeded_device. */
 int jne_run_batch(jne_context* ctx, const jne_request* reqs, int n_req, double* const* outs_device, void* stream);
+
+/* As jne_run_batch, then waits for the batch and reports each request's own
+ * status in status_out[i] (host, n_req ints): JNE_OK, or JNE_ERR_NUMERIC when
+ * some run of request i had a non-SPD S11 (its rows are NaN).  A failing
+ * request does not fail the others it shares a launch with: every request of
+ * the reference CLI's loop is its own simulation, which fails alone
+ * (src/data_storage/parallel_compute.rs:129-147, src/main.rs:85-136).  Returns
+ * JNE_OK when every request succeeded, the first failing request's code when
+ * some did, or the error that stopped the batch. */
+int jne_run_batch_status(jne_context* ctx, const jne_request* reqs, int n_req, double* const* outs_device,
+                         int* status_out, void* stream);
 
 /* Plans: a ragged batch prepared once (device tables and records inside the
  * context's budget) and captured into a CUDA graph; each jne_plan_launch

@@ -36,7 +36,7 @@ EXPORTS = (
     "jne_simulation_filename", "jne_simulation_run", "jne_simulation_run_models", "jne_percentiles",
     "jne_percentiles_device",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
-    "jne_run_batch", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
+    "jne_run_batch", "jne_run_batch_status", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
     "jne_server_open", "jne_server_submit", "jne_server_wait", "jne_server_fetch", "jne_server_close",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
@@ -154,6 +154,8 @@ def lib() -> ctypes.CDLL:
         L.jne_export_increments.argtypes = [vp, c_int, c_int, c_u64, c_u32, c_int, dp, ctypes.POINTER(c_u32)]
         L.jne_sync.argtypes = [vp]
         L.jne_run_batch.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp), vp]
+        L.jne_run_batch_status.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp),
+                                           ctypes.POINTER(c_int), vp]
         L.jne_plan_create.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.jne_plan_launch.argtypes = [vp, vp]
         L.jne_plan_destroy.argtypes = [vp]
@@ -307,6 +309,19 @@ class Engine:
         arr = self._requests(reqs)
         outs = (ctypes.c_void_p * len(reqs))(*[ctypes.c_void_p(p) for p in out_ptrs])
         self._check(self._L.jne_run_batch(self._h, arr, len(reqs), outs, ctypes.c_void_p(stream or 0)))
+
+    def run_batch_status(self, reqs: Sequence[dict], out_ptrs: Sequence[int],
+                         stream: Optional[int] = None) -> List[int]:
+        """jne_run_batch_status: the batch, waited for; returns each request's own status (JNE_OK or
+        JNE_ERR_NUMERIC), so a singular request fails alone.  Raises only when the batch itself fails."""
+        arr = self._requests(reqs)
+        outs = (ctypes.c_void_p * len(reqs))(*[ctypes.c_void_p(p) for p in out_ptrs])
+        st = (ctypes.c_int * max(1, len(reqs)))()
+        rc = self._L.jne_run_batch_status(self._h, arr, len(reqs), outs, st, ctypes.c_void_p(stream or 0))
+        codes = [int(st[i]) for i in range(len(reqs))]
+        if rc != JNE_OK and not any(c != JNE_OK for c in codes):
+            self._check(rc)
+        return codes
 
     def plan(self, reqs: Sequence[dict], out_ptrs: Sequence[int]) -> "Plan":
         """jne_plan_create: the batch captured into a CUDA graph, replayed by Plan.launch()."""

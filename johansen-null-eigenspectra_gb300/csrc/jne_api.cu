@@ -36,6 +36,7 @@ int jne_open(int device, unsigned long long mem_budget_bytes, jne_context** out)
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->fin_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   for (int i = 0; i < 2 && e == cudaSuccess; i++) {
     e = cudaEventCreateWithFlags(&c->ev_acc[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fin[i], cudaEventDisableTiming);
@@ -67,10 +68,12 @@ void jne_close(jne_context* c) {
   cudaFree(c->d_ent);
   cudaFree(c->d_ctab);
   cudaFree(c->d_status);
+  cudaFree(c->d_req_status);
   cudaFree(c->d_next_run);
   cudaFree(c->d_batch);
   cudaFree(c->d_qscratch);
   if (c->ev_in) cudaEventDestroy(c->ev_in);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   for (int i = 0; i < 2; i++) {
     cudaFree(c->d_reqs[i]);
     cudaFree(c->d_rtab[i]);

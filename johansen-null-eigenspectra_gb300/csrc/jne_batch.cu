@@ -34,10 +34,12 @@ int check_request(jne_context* c, const jne_request& r, double* out) {
 }
 
 // Host side of one ragged launch: device descriptors (request table and chunk
-// tables) for `pieces`, record slots laid out back to back from `mom`.
+// tables) for `pieces`, record slots laid out back to back from `mom`.  Each
+// piece reports its device status to its request's word (req_status[req]), or
+// to the context's word when req_status is null.
 void describe(jne_context* c, const jne_request* reqs, double* const* outs, const std::vector<Piece>& pieces,
               double* mom, const jne_chunk_time* d_tab, jne_ragged_req* hr, jne_chunk_time* ht, long long* total,
-              size_t* n_tab) {
+              size_t* n_tab, unsigned int* const* req_status = nullptr) {
   long long first = 0;
   size_t moff = 0, toff = 0;
   for (size_t i = 0; i < pieces.size(); i++) {
@@ -60,7 +62,8 @@ void describe(jne_context* c, const jne_request* reqs, double* const* outs, cons
     d.acc.chunk_tab = d_tab + toff;
     d.acc.mom = mom + moff;
     d.acc.mom_ld = p.n;
-    d.acc.status = c->d_status;
+    unsigned int* status = req_status ? req_status[p.req] : c->d_status;
+    d.acc.status = status;
     d.fin.model = r.model;
     d.fin.dim = r.dim;
     d.fin.steps = r.steps;
@@ -70,7 +73,7 @@ void describe(jne_context* c, const jne_request* reqs, double* const* outs, cons
     d.fin.mom = mom + moff;
     d.fin.mom_ld = p.n;
     d.fin.out = outs[p.req] + (size_t)p.offset * jne_eigen_count(r.model, r.dim);
-    d.fin.status = c->d_status;
+    d.fin.status = status;
     d.first = first;
     fill_chunk_table(r.steps, chunk, ht + toff);
     first += jne_units(r.dim, p.n);  // the kernel's items are units (packed pairs for small dims)
@@ -149,24 +152,24 @@ struct jne_plan {
   cudaEvent_t done = nullptr;
 };
 
-extern "C" {
-
-int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, void* stream) {
+int jne_detail::run_batch(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, cudaStream_t user,
+                          unsigned int* const* req_status) {
   if (!c) return JNE_ERR_ARG;
   if (n_req < 0 || (n_req > 0 && (!reqs || !outs))) return fail(c, JNE_ERR_ARG, "null request list");
   int rc;
   for (int i = 0; i < n_req; i++)
     if ((rc = check_request(c, reqs[i], outs[i]))) return rc;
-  cudaStream_t user = stream ? (cudaStream_t)stream : c->stream;
   if ((rc = join_in(c, user))) return rc;
   int last = -1;
+  bool seeded = false;  // some request finalizes on the context's second stream
   std::vector<int> ragged;
   for (int i = 0; i < n_req; i++) {
     if (reqs[i].n_runs == 0) continue;
     if (ragged_ok(reqs[i])) {
       ragged.push_back(i);
-    } else if ((rc = enqueue_seeded(c, reqs[i].model, reqs[i].dim, reqs[i].steps, reqs[i].base_seed,
-                                    reqs[i].seed_first, reqs[i].n_runs, reqs[i].precision, outs[i], &last))) {
+    } else if (seeded = true, (rc = enqueue_seeded(c, reqs[i].model, reqs[i].dim, reqs[i].steps, reqs[i].base_seed,
+                                    reqs[i].seed_first, reqs[i].n_runs, reqs[i].precision, outs[i], &last,
+                                    req_status ? req_status[i] : nullptr))) {
       return rc;
     }
   }
@@ -195,7 +198,8 @@ int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* co
       return rc;
     long long total = 0;
     size_t nt = 0;
-    describe(c, reqs, outs, pieces, c->d_momb[b], c->d_rtab[b], c->h_reqs[b], c->h_rtab[b], &total, &nt);
+    describe(c, reqs, outs, pieces, c->d_momb[b], c->d_rtab[b], c->h_reqs[b], c->h_rtab[b], &total, &nt,
+             req_status);
     if ((e = cudaMemcpyAsync(c->d_reqs[b], c->h_reqs[b], sizeof(jne_ragged_req) * pieces.size(),
                              cudaMemcpyHostToDevice, st)) != cudaSuccess ||
         (e = cudaMemcpyAsync(c->d_rtab[b], c->h_rtab[b], sizeof(jne_chunk_time) * nt, cudaMemcpyHostToDevice, st)) !=
@@ -213,7 +217,46 @@ int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* co
     c->fin_pending[b] = true;
     last = b;
   }
+  // the caller's stream waits for both streams' work: the ragged launches (the
+  // last one's event) and the FP64-path finalizes queued on the second stream
+  if (seeded && ((e = cudaEventRecord(c->ev_join, c->fin_stream)) != cudaSuccess ||
+                 (e = cudaStreamWaitEvent(user, c->ev_join, 0)) != cudaSuccess))
+    return cuda_fail(c, e, "stream join");
   return join_out(c, user, last);
+}
+
+extern "C" {
+
+int jne_run_batch(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, void* stream) {
+  if (!c) return JNE_ERR_ARG;
+  return run_batch(c, reqs, n_req, outs, stream ? (cudaStream_t)stream : c->stream, nullptr);
+}
+
+int jne_run_batch_status(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, int* status_out,
+                         void* stream) {
+  if (!c) return JNE_ERR_ARG;
+  if (n_req < 0 || (n_req > 0 && !status_out)) return fail(c, JNE_ERR_ARG, "null status list");
+  if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, JNE_ERR_CUDA, "cudaSetDevice failed");
+  if (n_req == 0) return JNE_OK;
+  int rc = ensure(c, &c->d_req_status, &c->req_status_cap, (size_t)n_req, "request status words");
+  if (rc) return rc;
+  cudaStream_t user = stream ? (cudaStream_t)stream : c->stream;
+  cudaError_t e = cudaMemsetAsync(c->d_req_status, 0, sizeof(unsigned int) * n_req, user);
+  if (e != cudaSuccess) return cuda_fail(c, e, "status reset");
+  std::vector<unsigned int*> words((size_t)n_req);
+  for (int i = 0; i < n_req; i++) words[(size_t)i] = c->d_req_status + i;
+  if ((rc = run_batch(c, reqs, n_req, outs, user, words.data()))) return rc;
+  std::vector<unsigned int> bits((size_t)n_req);
+  e = cudaMemcpyAsync(bits.data(), c->d_req_status, sizeof(unsigned int) * n_req, cudaMemcpyDeviceToHost, user);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(user);
+  if (e != cudaSuccess) return cuda_fail(c, e, "batch status");
+  int worst = JNE_OK;
+  for (int i = 0; i < n_req; i++) {
+    status_out[i] = status_code(bits[(size_t)i]);
+    if (status_out[i] != JNE_OK && worst == JNE_OK) worst = status_out[i];
+  }
+  if (worst != JNE_OK) return fail(c, worst, "some requests of the batch failed (see their status)");
+  return JNE_OK;
 }
 
 int jne_plan_create(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, jne_plan** out) {

@@ -35,6 +35,8 @@ struct jne_context {
   int4* d_ent = nullptr;
   size_t ent_cap = 0;
   unsigned int* d_status = nullptr;
+  unsigned int* d_req_status = nullptr;  // per-request status words (jne_run_batch_status)
+  size_t req_status_cap = 0;
   unsigned long long* d_next_run = nullptr;  // work counter of single-request mixed launches
   unsigned int* d_batch = nullptr;           // per-32-run completion counts of fused finalizes
   size_t batch_cap = 0;
@@ -48,7 +50,8 @@ struct jne_context {
   double* d_momb[2] = {nullptr, nullptr};
   size_t momb_cap[2] = {0, 0};
   unsigned long long batch_seq = 0;
-  cudaEvent_t ev_in = nullptr;  // joins a caller's stream into the context's streams
+  cudaEvent_t ev_in = nullptr;    // joins a caller's stream into the context's streams
+  cudaEvent_t ev_join = nullptr;  // the finalize stream's work of a batch -> the caller's stream
   // ragged batches: per record buffer, the device request table, chunk tables,
   // work counter, and pinned host staging for the tables
   jne_ragged_req* d_reqs[2] = {nullptr, nullptr};
@@ -248,9 +251,10 @@ inline int kernel_precision(int precision, int steps) {
 
 inline int finalize(jne_context* c, const jne_finalize_args& f, cudaStream_t st);
 
-// The finalize argument block of n runs of one request (records in mom).
+// The finalize argument block of n runs of one request (records in mom);
+// device status bits go to `status` (null: the context's status word).
 inline jne_finalize_args finalize_args(jne_context* c, int model, int dim, int steps, int n, const double* mom,
-                                       double* d_out) {
+                                       double* d_out, unsigned int* status = nullptr) {
   jne_finalize_args f{};
   f.model = model;
   f.dim = dim;
@@ -261,17 +265,18 @@ inline jne_finalize_args finalize_args(jne_context* c, int model, int dim, int s
   f.mom = mom;
   f.mom_ld = n;
   f.out = d_out;
-  f.status = c->d_status;
+  f.status = status ? status : c->d_status;
   return f;
 }
 
 // Moments of runs [seed_first, seed_first + n) into mom (leading dim n).  With
 // `fin`, the runs' eigenvalues are also produced on st: inside the mixed
 // kernel (each warp finalizes its runs), or by a finalize launch after the
-// FP64 kernel.
+// FP64 kernel.  The accumulation's status bits go to `status` (null: the
+// context's status word).
 inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t key0, uint32_t key1, uint32_t seed_first,
                       int n, int precision, const double* d_ext, double* mom, cudaStream_t st,
-                      const jne_finalize_args* fin = nullptr) {
+                      const jne_finalize_args* fin = nullptr, unsigned int* status = nullptr) {
   precision = kernel_precision(precision, steps);
   jne_accum_args a{};
   a.model = model;
@@ -286,7 +291,7 @@ inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t ke
   a.ext_inv_scale = std::sqrt((double)steps);
   a.mom = mom;
   a.mom_ld = n;
-  a.status = c->d_status;
+  a.status = status ? status : c->d_status;
   cudaError_t e;
   if (precision == JNE_PREC_FP64) {
     if (c->ent_model != model || c->ent_dim != dim) {
@@ -396,9 +401,11 @@ inline int join_out(jne_context* c, cudaStream_t user, int last) {
 // Mixed precision: the accumulation kernel finalizes its own runs, on
 // c->stream.  FP64: the finalize of a batch runs on c->fin_stream beside the
 // next batch's accumulation.  Events order the buffer reuse; *last receives
-// the record buffer of the final batch (its ev_fin marks the results).
+// the record buffer of the final batch (its ev_fin marks the results).  Device
+// status bits go to `status` (null: the context's status word).
 inline int enqueue_seeded(jne_context* c, int model, int dim, int steps, uint64_t base_seed, uint32_t seed_first,
-                          int64_t n_runs, int precision, double* out_device, int* last) {
+                          int64_t n_runs, int precision, double* out_device, int* last,
+                          unsigned int* status = nullptr) {
   const int k = jne_eigen_count(model, dim);
   uint32_t k0, k1;
   stream_key(base_seed, dim, &k0, &k1);
@@ -415,15 +422,16 @@ inline int enqueue_seeded(jne_context* c, int model, int dim, int steps, uint64_
       return cuda_fail(c, e, "stream wait");
     if ((rc = ensure(c, &c->d_momb[b], &c->momb_cap[b], (size_t)n * jne_record_slots(dim), "moment buffer")))
       return rc;
-    const jne_finalize_args fa = finalize_args(c, model, dim, steps, n, c->d_momb[b], out_device + (size_t)done * k);
+    const jne_finalize_args fa =
+        finalize_args(c, model, dim, steps, n, c->d_momb[b], out_device + (size_t)done * k, status);
     if (fused) {
       if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
-                           c->d_momb[b], st, &fa)))
+                           c->d_momb[b], st, &fa, status)))
         return rc;
       if ((e = cudaEventRecord(c->ev_fin[b], st)) != cudaSuccess) return cuda_fail(c, e, "event record");
     } else {
       if ((rc = accumulate(c, model, dim, steps, k0, k1, seed_first + (uint32_t)done, n, precision, nullptr,
-                           c->d_momb[b], st)))
+                           c->d_momb[b], st, nullptr, status)))
         return rc;
       if ((e = cudaEventRecord(c->ev_acc[b], st)) != cudaSuccess ||
           (e = cudaStreamWaitEvent(c->fin_stream, c->ev_acc[b], 0)) != cudaSuccess)
@@ -434,6 +442,18 @@ inline int enqueue_seeded(jne_context* c, int model, int dim, int steps, uint64_
     c->fin_pending[b] = true;
     *last = b;
   }
+  return JNE_OK;
+}
+
+// A ragged batch (jne_batch.cu): request i's device status bits go to
+// req_status[i] when req_status is given, else to the context's status word.
+int run_batch(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, cudaStream_t user,
+              unsigned int* const* req_status);
+
+// Converts a word of JNE_DEV_* bits into a status code.
+inline int status_code(unsigned int bits) {
+  if (bits & JNE_DEV_BAD_ARGS) return JNE_ERR_ARG;
+  if (bits & JNE_DEV_NOT_SPD) return JNE_ERR_NUMERIC;
   return JNE_OK;
 }
 

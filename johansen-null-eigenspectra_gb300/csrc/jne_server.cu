@@ -44,10 +44,16 @@ struct Job {
   std::vector<double> host;  // results, once finished
 };
 
+// One ragged launch in flight.  Each part (a slice of one job) reports its
+// device status to its own word of d_status, so a failing request marks only
+// itself, and a word is read only once its iteration's event has passed.
 struct Iteration {
   cudaEvent_t ev = nullptr;
   std::vector<std::pair<Job*, int64_t>> parts;  // job, runs it advanced
   bool busy = false;
+  unsigned int* d_status = nullptr;  // one word per part
+  size_t status_cap = 0;
+  std::vector<unsigned int> h_status;
 };
 
 }  // namespace
@@ -112,23 +118,21 @@ void finish_job(jne_server* s, Job* j, int status) {
   s->cv_done.notify_all();
 }
 
-// Completes the iteration in slot `i` (waits for its event) and retires jobs.
+// Completes the iteration in slot `i` (waits for its event) and retires jobs;
+// each job takes the status of its own part only.
 void retire(jne_server* s, int i) {
   Iteration& itr = s->it[i];
   if (!itr.busy) return;
+  const size_t np = itr.parts.size();
+  itr.h_status.assign(np, 0u);
   cudaError_t e = cudaEventSynchronize(itr.ev);
-  int st = JNE_OK;
-  if (e != cudaSuccess) st = JNE_ERR_CUDA;
-  if (st == JNE_OK) {
-    unsigned int v = 0;
-    if (cudaMemcpy(&v, s->ctx->d_status, sizeof v, cudaMemcpyDeviceToHost) == cudaSuccess && (v & JNE_DEV_NOT_SPD)) {
-      st = JNE_ERR_NUMERIC;
-      cudaMemset(s->ctx->d_status, 0, sizeof(unsigned int));
-    }
-  }
-  for (auto& p : itr.parts) {
+  if (e == cudaSuccess && np)
+    e = cudaMemcpy(itr.h_status.data(), itr.d_status, sizeof(unsigned int) * np, cudaMemcpyDeviceToHost);
+  for (size_t k = 0; k < np; k++) {
+    auto& p = itr.parts[k];
     Job* j = p.first;
     j->done += p.second;
+    const int st = e != cudaSuccess ? JNE_ERR_CUDA : status_code(itr.h_status[k]);
     if (st != JNE_OK && j->status == JNE_OK) j->status = st;
     if (j->done == j->req.n_runs) {
       {
@@ -202,6 +206,12 @@ void worker_loop(jne_server* s) {
     std::vector<jne_request> reqs;
     std::vector<double*> outs;
     Iteration& itr = s->it[slot];
+    // the iteration's status words, zeroed on the stream ahead of its launches
+    int rc = ensure(c, &itr.d_status, &itr.status_cap, std::max<size_t>(act.size(), 256), "server status words");
+    if (rc == JNE_OK && cudaMemsetAsync(itr.d_status, 0, sizeof(unsigned int) * act.size(), c->stream) != cudaSuccess)
+      rc = JNE_ERR_CUDA;
+    std::vector<unsigned int*> words(act.size());
+    for (size_t k = 0; k < act.size(); k++) words[k] = itr.d_status + k;
     for (Job* j : act) {
       const int64_t n = std::max<int64_t>(1, std::min<int64_t>(j->req.n_runs - j->next, share / j->req.steps));
       jne_request r = j->req;
@@ -214,7 +224,7 @@ void worker_loop(jne_server* s) {
       itr.parts.push_back({j, n});
     }
     // a failed slice still retires (with the error) through the iteration's event
-    int rc = jne_run_batch(c, reqs.data(), (int)reqs.size(), outs.data(), c->stream);
+    if (rc == JNE_OK) rc = run_batch(c, reqs.data(), (int)reqs.size(), outs.data(), c->stream, words.data());
     if (rc != JNE_OK)
       for (auto& p : itr.parts) p.first->status = rc;
     cudaEventRecord(itr.ev, c->stream);
@@ -348,7 +358,13 @@ int jne_server_close(jne_server* s) {
   }
   if (s->writer.joinable()) s->writer.join();
   for (auto& kv : s->finished) delete kv.second;
-  for (int i = 0; i < 2; i++) cudaEventDestroy(s->it[i].ev);
+  for (int i = 0; i < 2; i++) {
+    cudaEventDestroy(s->it[i].ev);
+    if (s->it[i].d_status) {
+      cudaFree(s->it[i].d_status);
+      s->ctx->in_use -= s->it[i].status_cap * sizeof(unsigned int);
+    }
+  }
   delete s;
   return JNE_OK;
 }

@@ -102,3 +102,39 @@ def test_ragged_mixed_requests_equal_single_requests_bit_for_bit(engine, jne):
     engine.sync()
     for r, o in zip(reqs, outs):
         assert np.array_equal(o.cpu().numpy(), _single(engine, jne, r)), r
+
+
+def test_singular_request_fails_alone(engine, jne):
+    """A request whose S11 is singular (steps = 1: F = B_0 = 0) in a batch with healthy ragged and FP64
+    requests: it alone reports JNE_ERR_NUMERIC (NaN rows); the others are JNE_OK and equal their
+    single-request results bit for bit."""
+    reqs = [MIX[0], dict(model=0, dim=3, steps=1, n_runs=5), MIX[1], MIX[6], MIX[2]]
+    outs = _outs(jne, reqs)
+    codes = engine.run_batch_status(reqs, [o.data_ptr() for o in outs])
+    assert codes == [jne.JNE_OK, jne.JNE_ERR_NUMERIC, jne.JNE_OK, jne.JNE_OK, jne.JNE_OK]
+    assert bool(outs[1].isnan().all())
+    for r, o, c in zip(reqs, outs, codes):
+        if c == jne.JNE_OK:
+            assert np.array_equal(o.cpu().numpy(), _single(engine, jne, r)), r
+    # the context's own status word is untouched: a plain sync reports nothing
+    engine.sync()
+    assert engine.run_batch_status(reqs[:1], [outs[0].data_ptr()]) == [jne.JNE_OK]
+
+
+def test_results_visible_on_the_caller_stream_without_sync(engine, jne):
+    """FP64-path requests finalize on the context's second stream, ragged ones on its first: work the
+    caller enqueues on its own stream after jne_run_batch sees both, with no jne_sync in between."""
+    import torch
+
+    reqs = [MIX[6], MIX[5], MIX[0], MIX[3]]
+    refs = [_single(engine, jne, r) for r in reqs]
+    st = torch.cuda.Stream()
+    for _ in range(3):
+        outs = _outs(jne, reqs)
+        engine.run_batch(reqs, [o.data_ptr() for o in outs], stream=st.cuda_stream)
+        with torch.cuda.stream(st):
+            copies = [o.clone() for o in outs]  # ordered after the batch on the caller's stream
+        st.synchronize()
+        for c, ref in zip(copies, refs):
+            assert np.array_equal(c.cpu().numpy(), ref)
+    engine.sync()

@@ -81,3 +81,24 @@ def test_admission_respects_the_budget(jne):
             assert done[big].status == jne.JNE_ERR_BUDGET
             assert done[ok].status == jne.JNE_OK
             assert srv.fetch(ok).shape == (100, 2)
+
+
+def test_singular_request_fails_alone_in_the_mix(jne):
+    """A singular request (steps = 1: S11 = 0) among healthy ones: only it reports JNE_ERR_NUMERIC, and
+    the others equal their results alone (each iteration's requests report to their own status words)."""
+    healthy = [MIX[0], MIX[1], MIX[5]]
+    with jne.Engine(0) as ref_eng, jne.Engine(0) as eng:
+        with jne.Server(eng, iter_work=50_000_000) as srv:
+            ids = [srv.submit(**healthy[0]), srv.submit(model=0, dim=4, steps=1, n_runs=64),
+                   srv.submit(**healthy[1]), srv.submit(**healthy[2])]
+            done = _collect(srv, len(ids))
+            assert done[ids[1]].status == jne.JNE_ERR_NUMERIC
+            with pytest.raises(jne.JneError) as ei:
+                srv.fetch(ids[1])
+            assert ei.value.code == jne.JNE_ERR_NUMERIC
+            for i, r in zip([ids[0], ids[2], ids[3]], healthy):
+                assert done[i].status == jne.JNE_OK
+                ref = ref_eng.eigs_seeded(r["model"], r["dim"], r["steps"], r.get("seed_first", 1), r["n_runs"],
+                                          precision=r.get("precision", jne.PREC_MIXED),
+                                          base_seed=r.get("base_seed", jne.DEFAULT_BASE_SEED))
+                assert np.array_equal(srv.fetch(i), ref), r
