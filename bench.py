@@ -352,6 +352,8 @@ def run_gpu(args, rank: int, world: int) -> None:
     ragged_tuned = (bench_ragged60(jne, torch, local, args.ragged_steps, tune=args.tune_err)
                     if args.ragged_steps > 0 and args.tune_err > 0 and rank == 0 else None)
     precision = bench_precision(jne, torch, local, args.c3_runs) if args.c3_runs > 0 and rank == 0 else None
+    tuned_single = (bench_tuned_single(jne, torch, local, args.tune_err)
+                    if args.tune_err > 0 and rank == 0 else None)
     # all five models of the same seeds from one pass over the paths (jne_eigs_seeded_models): the path of a
     # seed does not depend on the model, so one accumulation serves five finalizes; host outputs
     eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, min(R, 20_000), precision=jne.PREC_MIXED)
@@ -408,7 +410,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
             "gpu_launches": acc_n + fin_n,
             "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
-            "ragged60": ragged, "ragged60_tuned": ragged_tuned, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
+            "ragged60": ragged, "ragged60_tuned": ragged_tuned, "tuned_single": tuned_single, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
             "cpu_baseline": cpu, "clocks": clocks,
         }))
     eng.close()
@@ -428,14 +430,50 @@ def ragged60_requests(seed: int = 0xC4):
 
 
 def tune_classes(eng, classes, max_rel_err: float) -> dict:
-    """Chunk autotuner over the (dim, steps) classes of a workload; returns {"dim x 2^b": chunk}."""
+    """Autotuner over the (dim, steps) classes of a workload (512 sample runs per model, 16,384-run timed
+    launches); returns {"dim x 2^b": chunk} -- the ragged kernel takes the chunk of each tuned shape."""
     out = {}
     for dim, steps in sorted(set(classes)):
         if steps >= 256:
-            chunk, _ = eng.autotune_chunk(dim, steps, max_rel_err=max_rel_err, sample_runs=256)
-            out[f"{dim}x{1 << (steps.bit_length() - 1)}"] = chunk
+            best, _ = eng.autotune(dim, steps, max_rel_err=max_rel_err, sample_runs=512, time_runs=16384)
+            out[f"{dim}x{1 << (steps.bit_length() - 1)}"] = best["chunk"]
     eng.set_chunk(-1)  # CHUNK_TUNED
     return out
+
+
+def bench_tuned_single(jne, torch, local: int, max_rel_err: float, shapes=((2, 1000), (6, 1000), (12, 10_000))):
+    """Single requests (model 0) with the default launch shape and with the autotuned one (2,000 sample runs
+    per model for the error bound, timed candidates), device outputs, CUDA events; plus the tuner's table."""
+    out = []
+    with jne.Engine(local) as eng:
+        st = torch.cuda.Stream()
+        for dim, steps in shapes:
+            best, table = eng.autotune(dim, steps, max_rel_err=max_rel_err, sample_runs=2000)
+            runs = int(min(4_000_000, max(65_536, 4e10 / (steps * (dim + 3)))))
+            buf = torch.empty((runs, dim), dtype=torch.float64, device="cuda")
+            rates = {}
+            for mode in (0, -1):  # default rule, then CHUNK_TUNED
+                eng.set_chunk(mode)
+                eng.eigs_seeded_device(0, dim, steps, 1, runs, buf.data_ptr(), precision=jne.PREC_MIXED,
+                                       stream=st.cuda_stream)
+                eng.sync()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                for _ in range(3):
+                    eng.eigs_seeded_device(0, dim, steps, 1, runs, buf.data_ptr(), precision=jne.PREC_MIXED,
+                                           stream=st.cuda_stream)
+                b.record(st)
+                b.synchronize()
+                eng.sync()
+                rates["default" if mode == 0 else "tuned"] = 3 * runs / (a.elapsed_time(b) * 1e-3)
+            eng.set_chunk(0)
+            out.append({"dim": dim, "steps": steps, "runs": runs, "default_runs_per_s": rates["default"],
+                        "tuned_runs_per_s": rates["tuned"], "gain": rates["tuned"] / rates["default"],
+                        "chosen": best, "table": table})
+    return {"max_rel_err": max_rel_err, "shapes": out,
+            "note": "default: chunk rule, 4 blocks per SM, two runs per warp for dims <= 4; tuned: the fastest "
+                    "measured shape whose chunk meets the bound on 2,000 runs per model"}
 
 
 def bench_ragged60(jne, torch, local: int, steps: int, tune: float = 0.0) -> dict:

@@ -73,22 +73,45 @@ const char* jne_last_error(const jne_context* ctx);
 
 /* Steps per FP32 chunk of the mixed kernel: a multiple of 32 up to 8192, or 0
  * (the default) for the largest power of two <= steps/16 in [32, 512], or
- * JNE_CHUNK_TUNED for the lengths jne_autotune_chunk chose (the default rule
- * for classes it has not tuned). */
+ * JNE_CHUNK_TUNED for the launch shapes jne_autotune chose (chunk, kernel
+ * variant, packing; the default rule for classes it has not tuned). */
 #define JNE_CHUNK_TUNED (-1)
 int jne_set_chunk(jne_context* ctx, int chunk);
 
-/* Autotuner of the mixed kernel's chunk length, the speed / accuracy knob of
- * the mixed path: longer chunks mean fewer FP64-exact merges (faster) and more
- * FP32 accumulation per chunk (less accurate).  For the class of (dim, steps)
- * -- steps in [2^b, 2^(b+1)), tuned at 2^b where errors are largest -- it runs
- * seeds 1..sample_runs of all five models with the FP64 kernel and with each
- * candidate chunk 32, 64, ... (at most 1024 and half the steps), and keeps the
- * longest chunk up to which every candidate's largest error stays within
- * max_rel_err: max-eigenvalue and trace differences relative to max(value, 1).
- * The choice is stored in ctx for JNE_CHUNK_TUNED.  Classes below
- * JNE_MIXED_MIN_STEPS run the FP64 kernel and are not tuned (JNE_ERR_ARG).
- * chunk_out / err_out (the chosen chunk's error) may be null. */
+/* The mixed single-request kernel's variant outside JNE_CHUNK_TUNED mode:
+ * blocks_per_sm 4 (the default, 128 registers a thread) or 6 (80), and for
+ * dims up to 4 pack = 1 (the default, two runs per warp) or 0 (one).  0 for
+ * either keeps its default.  Speed only: every variant gives the same bits.
+ * No counterpart in the reference. */
+int jne_set_launch_shape(jne_context* ctx, int blocks_per_sm, int pack);
+
+/* One candidate launch shape of the mixed kernel, as jne_autotune measured it. */
+typedef struct jne_tune_entry {
+  int chunk;          /* steps per FP32 chunk */
+  int blocks_per_sm;  /* kernel variant: 4 (128 registers a thread) or 6 (80) */
+  int pack;           /* dims <= 4: 1 = two runs per warp, 0 = one */
+  double max_rel_err; /* worst max-eig / trace error vs FP64 on the sample (five models), relative to max(value, 1) */
+  double ms;          /* device time of one launch of time_runs runs (model 0); < 0: not timed (over the bound) */
+} jne_tune_entry;
+
+/* Autotuner of the mixed kernel (no counterpart in the reference, whose only
+ * knob is its thread count, src/cli.rs:311-329).  For the class of
+ * (dim, steps) -- steps in [2^b, 2^(b+1)), tuned at 2^b where errors are
+ * largest -- it runs seeds 1..sample_runs of all five models with the FP64
+ * kernel and with each chunk 32, 64, ... (at most 1024 and half the steps) up
+ * to the first over max_rel_err; then it times, with CUDA events, one launch of
+ * time_runs runs (0: sized for about 20-60 ms) for every shape of every chunk
+ * within the bound: blocks per SM 4 or 6, and one or two runs per warp for dims
+ * up to 4.  The fastest shape is stored in ctx for JNE_CHUNK_TUNED and written
+ * to *chosen; the measured candidates go to table (up to table_cap, *n_table of
+ * them).  Only the chunk changes results: shapes of one chunk give the same
+ * bits.  Classes below JNE_MIXED_MIN_STEPS run the FP64 kernel and are not
+ * tuned (JNE_ERR_ARG).  table, n_table and chosen may be null. */
+int jne_autotune(jne_context* ctx, int dim, int steps, double max_rel_err, int sample_runs, int64_t time_runs,
+                 jne_tune_entry* table, int table_cap, int* n_table, jne_tune_entry* chosen);
+
+/* jne_autotune with time_runs sized automatically and no table: the chosen
+ * (fastest admissible) chunk and its error.  chunk_out / err_out may be null. */
 int jne_autotune_chunk(jne_context* ctx, int dim, int steps, double max_rel_err, int sample_runs, int* chunk_out,
                        double* err_out);
 

@@ -32,6 +32,7 @@ EXPORTS = (
     "jne_version", "jne_eigen_count", "jne_open", "jne_close", "jne_last_error", "jne_set_chunk",
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
     "jne_export_increments", "jne_profile", "jne_profile_read", "jne_probe_rates", "jne_sync", "jne_autotune_chunk",
+    "jne_autotune", "jne_set_launch_shape",
     "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
     "jne_simulation_filename", "jne_simulation_run", "jne_simulation_run_models", "jne_percentiles",
     "jne_percentiles_device",
@@ -48,6 +49,16 @@ class Request(ctypes.Structure):
 
     _fields_ = [("model", ctypes.c_int), ("dim", ctypes.c_int), ("steps", ctypes.c_int), ("precision", ctypes.c_int),
                 ("base_seed", ctypes.c_uint64), ("seed_first", ctypes.c_uint32), ("n_runs", ctypes.c_int64)]
+
+
+class TuneEntry(ctypes.Structure):
+    """jne_tune_entry: one launch shape the autotuner measured."""
+
+    _fields_ = [("chunk", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("pack", ctypes.c_int),
+                ("max_rel_err", ctypes.c_double), ("ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class Completion(ctypes.Structure):
@@ -146,6 +157,7 @@ def lib() -> ctypes.CDLL:
         L.jne_last_error.argtypes = [vp]
         L.jne_last_error.restype = ctypes.c_char_p
         L.jne_set_chunk.argtypes = [vp, c_int]
+        L.jne_set_launch_shape.argtypes = [vp, c_int, c_int]
         L.jne_eigs_from_increments.argtypes = [vp, c_int, c_int, c_int, dp, c_int, c_int, dp]
         L.jne_eigs_seeded.argtypes = [vp, c_int, c_int, c_int, c_u64, c_u32, c_i64, c_int, dp]
         L.jne_eigs_seeded_device.argtypes = [vp, c_int, c_int, c_int, c_u64, c_u32, c_i64, c_int, vp, vp]
@@ -169,6 +181,8 @@ def lib() -> ctypes.CDLL:
         L.jne_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), c_int]
         L.jne_probe_rates.argtypes = [vp, dp]
         L.jne_autotune_chunk.argtypes = [vp, c_int, c_int, ctypes.c_double, c_int, ctypes.POINTER(c_int), dp]
+        L.jne_autotune.argtypes = [vp, c_int, c_int, ctypes.c_double, c_int, c_i64, ctypes.POINTER(TuneEntry), c_int,
+                                   ctypes.POINTER(c_int), ctypes.POINTER(TuneEntry)]
         L.jne_percentiles_device.argtypes = [vp, vp, c_i64, c_int, c_int, dp, c_int, dp, vp]
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
         L.jne_dat_open.argtypes = [ctypes.c_char_p, c_int, c_int, c_u32, ctypes.POINTER(vp), i64p]
@@ -229,9 +243,25 @@ class Engine:
         """Steps per FP32 chunk of the mixed kernel: 0 (default rule), CHUNK_TUNED or a multiple of 32 up to 8192."""
         self._check(self._L.jne_set_chunk(self._h, chunk))
 
+    def set_launch_shape(self, blocks_per_sm: int = 4, pack: int = 1) -> None:
+        """The mixed kernel variant outside CHUNK_TUNED mode: 4 or 6 blocks per SM; for dims <= 4 two runs
+        per warp (pack=1) or one (pack=0).  Speed only: the same bits."""
+        self._check(self._L.jne_set_launch_shape(self._h, blocks_per_sm, pack))
+
+    def autotune(self, dim: int, steps: int, max_rel_err: float = 1e-6, sample_runs: int = 2000,
+                 time_runs: int = 0) -> Tuple[dict, List[dict]]:
+        """jne_autotune: the fastest launch shape (chunk, blocks per SM, packing) whose chunk keeps the error
+        vs the FP64 kernel within max_rel_err on the sample, for steps in [2^b, 2^(b+1)); used after
+        set_chunk(CHUNK_TUNED).  Returns (chosen shape, every measured candidate) as dicts."""
+        table = (TuneEntry * 64)()
+        n, best = ctypes.c_int(), TuneEntry()
+        self._check(self._L.jne_autotune(self._h, dim, steps, float(max_rel_err), sample_runs, time_runs, table, 64,
+                                         ctypes.byref(n), ctypes.byref(best)))
+        return best.as_dict(), [table[i].as_dict() for i in range(n.value)]
+
     def autotune_chunk(self, dim: int, steps: int, max_rel_err: float = 5e-7, sample_runs: int = 512) -> Tuple[int, float]:
-        """The longest chunk whose error vs the FP64 kernel stays within max_rel_err on the sample,
-        for steps in [2^b, 2^(b+1)); used after set_chunk(CHUNK_TUNED).  Returns (chunk, its error)."""
+        """The fastest admissible chunk of jne_autotune (its shape is stored too), for steps in
+        [2^b, 2^(b+1)); used after set_chunk(CHUNK_TUNED).  Returns (chunk, its error)."""
         ch, err = ctypes.c_int(), np.zeros(1)
         self._check(self._L.jne_autotune_chunk(self._h, dim, steps, float(max_rel_err), sample_runs, ctypes.byref(ch),
                                                _dp(err)))

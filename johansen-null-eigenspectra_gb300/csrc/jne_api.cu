@@ -101,6 +101,15 @@ int jne_set_chunk(jne_context* c, int chunk) {
   return JNE_OK;
 }
 
+int jne_set_launch_shape(jne_context* c, int blocks_per_sm, int pack) {
+  if (!c) return JNE_ERR_ARG;
+  if ((blocks_per_sm != 0 && blocks_per_sm != 4 && blocks_per_sm != 6) || pack < 0 || pack > 1)
+    return fail(c, JNE_ERR_ARG, "blocks_per_sm must be 0, 4 or 6 and pack 0 or 1");
+  c->force.blocks_per_sm = blocks_per_sm ? blocks_per_sm : 4;
+  c->force.pack = pack;
+  return JNE_OK;
+}
+
 int jne_profile(jne_context* c, int enable) {
   if (!c) return JNE_ERR_ARG;
   c->profiling = enable != 0;

@@ -176,6 +176,8 @@ struct jne_accum_args {
                                  // assignment, or null for a fixed stride per warp
   unsigned int* batch_done;      // mixed kernel with a fused finalize: zeroed count of
                                  // accumulated runs per 32-run batch (ceil(n_runs / 32))
+  int blocks_per_sm;             // mixed kernel variant: 4 (0 = default) or 6
+  int pack;                      // mixed kernel, dims <= 4: >= 0 two runs per warp, < 0 one
 };
 
 // Status bits a kernel may raise (never a trap).

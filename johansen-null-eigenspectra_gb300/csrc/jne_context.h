@@ -11,13 +11,21 @@
 #include "../../include/jne.h"
 #include "jne_kernels.h"
 
+// The mixed kernel's launch shape for one (dim, class of steps): chunk length,
+// blocks per SM of the kernel variant (4 or 6) and whether dims <= 4 pack two
+// runs per warp.  Only the chunk changes the arithmetic.
+struct jne_shape {
+  int chunk = 0, blocks_per_sm = 4, pack = 1;
+};
+
 struct jne_context {
   int device = 0;
   int sms = 0;
   unsigned long long budget = 0;
   unsigned long long in_use = 0;
   int chunk = 0;  // 0: chunk length chosen from the step count; JNE_CHUNK_TUNED: tuned table
-  std::map<std::pair<int, int>, int> tuned_chunk;  // (dim, floor(log2 steps)) -> chunk
+  std::map<std::pair<int, int>, jne_shape> tuned;  // (dim, floor(log2 steps)) -> shape
+  jne_shape force;  // while tuning: blocks per SM and packing of every single-request launch
   jne_chunk_time* d_ctab = nullptr;
   size_t ctab_cap = 0;
   std::vector<jne_chunk_time> h_ctab;
@@ -179,10 +187,23 @@ inline int steps_bucket(int steps) {
 inline int chunk_for(const jne_context* c, int dim, int steps) {
   if (c->chunk > 0) return c->chunk;
   if (c->chunk == JNE_CHUNK_TUNED) {
-    const auto it = c->tuned_chunk.find({dim, steps_bucket(steps)});
-    if (it != c->tuned_chunk.end()) return it->second;
+    const auto it = c->tuned.find({dim, steps_bucket(steps)});
+    if (it != c->tuned.end()) return it->second.chunk;
   }
   return adaptive_chunk(steps);
+}
+
+// The single-request kernel variant for (dim, steps): the tuned one in
+// JNE_CHUNK_TUNED mode, else 4 blocks per SM with packed small dims (or the
+// tuner's candidate while it times one).
+inline jne_shape shape_for(const jne_context* c, int dim, int steps) {
+  jne_shape s = c->force;
+  if (c->chunk == JNE_CHUNK_TUNED) {
+    const auto it = c->tuned.find({dim, steps_bucket(steps)});
+    if (it != c->tuned.end()) s = it->second;
+  }
+  s.chunk = chunk_for(c, dim, steps);
+  return s;
 }
 
 inline bool valid_model_dim(int model, int dim) { return model >= 0 && model <= 4 && dim >= 1 && dim <= JNE_MAX_DIM; }
@@ -325,6 +346,9 @@ inline int accumulate(jne_context* c, int model, int dim, int steps, uint32_t ke
     c->ctab_chunk = a.chunk;
     }
     a.chunk_tab = c->d_ctab;
+    const jne_shape shape = shape_for(c, dim, steps);
+    a.blocks_per_sm = d_ext ? 4 : shape.blocks_per_sm;
+    a.pack = d_ext || shape.pack ? 0 : -1;
     // warps take runs from a counter, so blocks that start late (behind a
     // concurrent finalize) take fewer runs instead of leaving a tail
     e = cudaMemsetAsync(c->d_next_run, 0, sizeof(unsigned long long), st);

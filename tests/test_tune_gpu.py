@@ -1,6 +1,8 @@
-"""The chunk-length autotuner: the chunk it keeps meets the error bound on its
-sample, the tuned mode reproduces the fixed-chunk results exactly, and the
-ragged path uses the tuned lengths too."""
+"""The mixed kernel's launch shapes and their autotuner: every shape (blocks
+per SM, one or two runs per warp) gives the same bits; the tuner keeps the
+fastest measured shape whose chunk meets the error bound on its sample; the
+tuned mode reproduces the fixed-chunk results exactly, and the ragged path uses
+the tuned chunk lengths too."""
 import numpy as np
 import pytest
 
@@ -9,14 +11,31 @@ from conftest import normwise_err
 pytestmark = pytest.mark.gpu
 
 
-def test_tuner_respects_the_bound_and_grows_with_it(jne):
+@pytest.mark.parametrize("dim,steps", [(2, 700), (3, 1300), (7, 900), (12, 2000)])
+def test_every_launch_shape_gives_the_same_bits(jne, dim, steps):
     with jne.Engine(0) as eng:
-        tight, e_tight = eng.autotune_chunk(6, 3000, max_rel_err=5e-7, sample_runs=256)
-        loose, e_loose = eng.autotune_chunk(6, 3000, max_rel_err=1e-3, sample_runs=256)
-    assert tight in (32, 64, 128, 256, 512, 1024) and loose in (32, 64, 128, 256, 512, 1024)
-    assert tight == 32 or e_tight <= 5e-7
-    assert e_loose <= 1e-3 and loose >= tight
-    assert loose == 1024  # 2048 steps (the class's lower edge) allow chunks up to 1024
+        ref = eng.eigs_seeded(4, dim, steps, 1, 257, precision=jne.PREC_MIXED)
+        for bps in (4, 6):
+            for pack in (1, 0):
+                eng.set_launch_shape(bps, pack)
+                got = eng.eigs_seeded(4, dim, steps, 1, 257, precision=jne.PREC_MIXED)
+                assert np.array_equal(got, ref), (bps, pack)
+
+
+def test_tuner_keeps_the_fastest_shape_within_the_bound(jne):
+    with jne.Engine(0) as eng:
+        best, table = eng.autotune(6, 3000, max_rel_err=5e-7, sample_runs=256, time_runs=65536)
+        timed = [t for t in table if t["ms"] >= 0]
+        assert timed and all(t["max_rel_err"] <= 5e-7 or t["chunk"] == 32 for t in timed)
+        assert all(t["max_rel_err"] > 5e-7 for t in table if t["ms"] < 0)
+        assert best["ms"] == min(t["ms"] for t in timed)
+        assert {(t["blocks_per_sm"], t["pack"]) for t in timed} == {(4, 1), (6, 1)}  # dim 6: never packed
+        loose, table = eng.autotune(3, 3000, max_rel_err=1e-3, sample_runs=256, time_runs=65536)
+        # 2048 steps (the class's lower edge) allow chunks up to 1024, all within 1e-3; dim 3 also times
+        # the unpacked shapes
+        assert sorted({t["chunk"] for t in table if t["ms"] >= 0}) == [32, 64, 128, 256, 512, 1024]
+        assert {(t["blocks_per_sm"], t["pack"]) for t in table} == {(4, 1), (4, 0), (6, 1), (6, 0)}
+        assert loose["max_rel_err"] <= 1e-3
 
 
 def test_tuned_mode_equals_the_fixed_chunk(jne):
@@ -57,4 +76,8 @@ def test_tuner_arguments(jne):
         for args in ((12, 200, 5e-7, 64), (13, 5000, 5e-7, 64), (4, 5000, 0.0, 64), (4, 5000, 5e-7, 0)):
             with pytest.raises(jne.JneError) as ei:
                 eng.autotune_chunk(*args)
+            assert ei.value.code == jne.JNE_ERR_ARG
+        for shape in ((5, 1), (4, 2), (8, 0)):
+            with pytest.raises(jne.JneError) as ei:
+                eng.set_launch_shape(*shape)
             assert ei.value.code == jne.JNE_ERR_ARG
