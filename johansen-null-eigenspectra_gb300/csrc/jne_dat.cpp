@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -347,16 +348,52 @@ int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs,
       off[(size_t)p + 1] = off[(size_t)p] + bytes;
     }
     w->rec.resize(off[(size_t)parts]);
-    if (parts == 1) {
-      encode(b0, b1, w->rec.data());
-    } else {
-      std::vector<std::thread> th;
-      for (int p = 0; p < parts; p++)
+    // parts run on threads; a part whose thread cannot be started is encoded
+    // here instead (no exception leaves the C ABI)
+    std::vector<std::thread> th;
+    int started = 0;
+    for (int p = 1; p < parts; p++) {
+      try {
         th.emplace_back([&, p]() { encode(part_lo(p), part_lo(p + 1), w->rec.data() + off[(size_t)p]); });
-      for (std::thread& t : th) t.join();
+        started = p;
+      } catch (const std::system_error&) {
+        break;
+      }
     }
-    if (std::fwrite(w->rec.data(), 1, w->rec.size(), w->f) != w->rec.size())
-      return dat_fail(JNE_ERR_IO, "record write failed");
+    encode(part_lo(0), part_lo(1), w->rec.data());
+    for (int p = started + 1; p < parts; p++) encode(part_lo(p), part_lo(p + 1), w->rec.data() + off[(size_t)p]);
+    for (std::thread& t : th) t.join();
+    // The block goes straight to the file descriptor (after what stdio holds),
+    // so a short write is seen here with its exact length, not later at close.
+    if (std::fflush(w->f) != 0) return dat_fail(JNE_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+    const int fd = fileno(w->f);
+    const off_t start = lseek(fd, 0, SEEK_CUR);
+    size_t wrote = 0;
+    int err = 0;
+    while (wrote < w->rec.size()) {
+      const ssize_t r = ::write(fd, w->rec.data() + wrote, w->rec.size() - wrote);
+      if (r < 0 && errno == EINTR) continue;
+      if (r <= 0) {
+        err = r < 0 ? errno : EIO;
+        break;
+      }
+      wrote += (size_t)r;
+    }
+    if (wrote != w->rec.size()) {
+      // Keep the file and the count in step: count the whole records the
+      // short write holds and cut the file back to their end, so the file
+      // never ends in a partial record.
+      int64_t whole = 0;
+      size_t bytes = 0;
+      for (int64_t r = b0; r < b1 && bytes + rec_size(seeds[r]) <= wrote; r++) {
+        bytes += rec_size(seeds[r]);
+        whole++;
+      }
+      if (start >= 0 && ftruncate(fd, start + (off_t)bytes) == 0) lseek(fd, start + (off_t)bytes, SEEK_SET);
+      w->count += whole;
+      return dat_fail(JNE_ERR_IO, "record write failed after " + std::to_string(w->count) + " records: " +
+                                      std::strerror(err));
+    }
     w->count += b1 - b0;
   }
   return JNE_OK;
@@ -440,7 +477,11 @@ int remaining_seeds(const std::string& dir, int model, int dim, int steps, int64
   }
   // seeds 1..num_runs not in the file, by one merge walk over the sorted seeds
   remaining->clear();
-  remaining->reserve((size_t)num_runs);
+  const int64_t in_range = std::lower_bound(done.begin(), done.end(), (uint64_t)num_runs + 1 > 0xFFFFFFFFull
+                                                                          ? 0xFFFFFFFFu
+                                                                          : (uint32_t)(num_runs + 1)) -
+                           std::lower_bound(done.begin(), done.end(), 1u);
+  remaining->reserve((size_t)std::max<int64_t>(0, num_runs - in_range));
   size_t d = 0;
   for (int64_t s = 1; s <= num_runs; s++) {
     while (d < done.size() && done[d] < (uint32_t)s) d++;

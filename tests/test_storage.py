@@ -180,3 +180,49 @@ def test_large_file_parallel_decode(jne, tmp, finished):
     assert (model, dim, steps) == (1, 2, 64)
     assert np.array_equal(np.asarray(recs.seeds, dtype=np.uint32), seeds)
     assert np.array_equal(recs.eigs, eigs)
+
+
+_SHORT_WRITE_CHILD = r"""
+import os, resource, signal, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import __graft_entry__ as entry
+jne = entry.load_package()
+path, limit = sys.argv[2], int(sys.argv[3])
+w = jne.DatWriter(path, 0, 2, 100)           # header written before the limit applies
+w.append(range(1, 3), np.ones((2, 2)))
+signal.signal(signal.SIGXFSZ, signal.SIG_IGN)  # a write past the limit fails with EFBIG instead
+resource.setrlimit(resource.RLIMIT_FSIZE, (limit, limit))
+n = 100_000                                   # 2.7 MB of records in one block
+try:
+    w.append(range(3, 3 + n), np.arange(2 * n, dtype=float).reshape(n, 2))
+except jne.DatError as e:
+    print("IOERR", e.code)
+w.abandon()
+"""
+
+
+def test_short_write_leaves_whole_records(jne, tmp):
+    """A block write that the file system cuts short (here a file-size limit) leaves the file at a record
+    boundary: every record in it reads back whole, with no partial record at the end."""
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+
+    path = os.path.join(tmp, "short.dat")
+    limit = 100_003  # not a record boundary (records of dim 2 take 19-22 bytes)
+    out = subprocess.run([sys.executable, "-c", _SHORT_WRITE_CHILD, ROOT, path, str(limit)],
+                         capture_output=True, text=True, timeout=120)
+    assert f"IOERR {jne.JNE_ERR_IO}" in out.stdout, out.stdout + out.stderr
+    size = os.path.getsize(path)
+    assert size <= limit
+    recs, model, dim, steps = jne.read_dat(path)  # no trailer: read by scanning
+    n = len(recs.seeds)
+    assert n > 1000
+    assert list(recs.seeds[:3]) == [1, 2, 3]
+    assert np.array_equal(recs.eigs[2:], np.arange(2 * (n - 2), dtype=float).reshape(n - 2, 2))
+    # the file ends exactly after the last record: 18-byte header + records of 1-3 seed bytes + 1 + 16
+    seeds = np.asarray(recs.seeds, dtype=np.int64)
+    seed_bytes = 1 + (seeds >= 1 << 7) + (seeds >= 1 << 14) + (seeds >= 1 << 21)
+    assert size == 18 + int(np.sum(seed_bytes + 17))
