@@ -197,6 +197,40 @@ int jne_run_batch(jne_context* ctx, const jne_request* reqs, int n_req, double* 
 int jne_run_batch_status(jne_context* ctx, const jne_request* reqs, int n_req, double* const* outs_device,
                          int* status_out, void* stream);
 
+/* ---- streaming sink: the batch with its results delivered to host code ----
+ * The reference computes each run and sends (seed, eigenvalues) over a channel
+ * to a writer thread that appends it to the simulation's file
+ * (src/data_storage/parallel_compute.rs:14-41, thread_manager.rs:25-92,
+ * writer.rs:206-259).  Here a batch is computed in rounds of ragged launches
+ * and each round's results reach `write` on the calling thread while the GPU
+ * computes the next round. */
+typedef struct jne_sink {
+  /* n consecutive results of request `req` (its index in the batch): seeds
+   * seed_first .. seed_first + n - 1, k eigenvalues each (descending,
+   * run-major, host memory valid during the call).  A request's results arrive
+   * in seed order.  status: JNE_OK, or JNE_ERR_NUMERIC when some of these rows
+   * are NaN (S11 not positive definite).  A non-zero return stops the batch, and
+   * jne_run_batch_sink returns it. */
+  int (*write)(void* user, int req, uint32_t seed_first, int64_t n, int k, const double* eigs, int status);
+  void* user;
+} jne_sink;
+
+/* The batch of jne_run_batch, streamed to `sink`.  Synchronous: returns when
+ * every result has been delivered (JNE_OK, or JNE_ERR_NUMERIC when some rows
+ * were NaN), when the sink stops it (its code), or on an error.  Rounds hold up
+ * to 2^20 runs (fewer under a small budget). */
+int jne_run_batch_sink(jne_context* ctx, const jne_request* reqs, int n_req, const jne_sink* sink);
+
+/* A sink that appends each request's records to its simulation file
+ * <data_dir>/eigenvalues_model{m}_dim{d}_steps{T}.dat (data_dir null or empty:
+ * "data", created on demand; requests with the same (model, dim, steps) share
+ * the file; an existing file is appended to as jne_dat_open does).  Results
+ * with a non-OK status stop the batch with that status (the reference's writer
+ * never sees such a run: its sort panics first).  jne_dat_sink_close writes the
+ * EOF trailers (finish != 0) or leaves the files as an interrupted run does. */
+int jne_dat_sink_open(const char* data_dir, const jne_request* reqs, int n_req, jne_sink* out);
+int jne_dat_sink_close(jne_sink* sink, int finish);
+
 /* Plans: a ragged batch prepared once (device tables and records inside the
  * context's budget) and captured into a CUDA graph; each jne_plan_launch
  * replays it asynchronously on `stream`.  Requests must be mixed precision with

@@ -37,7 +37,8 @@ EXPORTS = (
     "jne_simulation_filename", "jne_simulation_run", "jne_simulation_run_models", "jne_percentiles",
     "jne_percentiles_device",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
-    "jne_run_batch", "jne_run_batch_status", "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
+    "jne_run_batch", "jne_run_batch_status", "jne_run_batch_sink", "jne_dat_sink_open", "jne_dat_sink_close",
+    "jne_plan_create", "jne_plan_launch", "jne_plan_destroy",
     "jne_server_open", "jne_server_submit", "jne_server_wait", "jne_server_fetch", "jne_server_close",
 )
 KERNEL_KINDS = ("accum_fp64", "accum_mixed", "finalize", "export")
@@ -59,6 +60,16 @@ class TuneEntry(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+SINK_WRITE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int64,
+                              ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int)
+
+
+class Sink(ctypes.Structure):
+    """jne_sink: a write callback and its user pointer."""
+
+    _fields_ = [("write", SINK_WRITE), ("user", ctypes.c_void_p)]
 
 
 class Completion(ctypes.Structure):
@@ -168,6 +179,9 @@ def lib() -> ctypes.CDLL:
         L.jne_run_batch.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp), vp]
         L.jne_run_batch_status.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp),
                                            ctypes.POINTER(c_int), vp]
+        L.jne_run_batch_sink.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(Sink)]
+        L.jne_dat_sink_open.argtypes = [ctypes.c_char_p, ctypes.POINTER(Request), c_int, ctypes.POINTER(Sink)]
+        L.jne_dat_sink_close.argtypes = [ctypes.POINTER(Sink), c_int]
         L.jne_plan_create.argtypes = [vp, ctypes.POINTER(Request), c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.jne_plan_launch.argtypes = [vp, vp]
         L.jne_plan_destroy.argtypes = [vp]
@@ -352,6 +366,31 @@ class Engine:
         if rc != JNE_OK and not any(c != JNE_OK for c in codes):
             self._check(rc)
         return codes
+
+    def run_batch_sink(self, reqs: Sequence[dict], write) -> None:
+        """jne_run_batch_sink: the batch streamed to write(req, seed_first, eigs (n x k array, a copy), status),
+        called in seed order per request; a non-zero int return stops the batch (raised as JneError)."""
+        arr = self._requests(reqs)
+
+        def cb(user, req, seed_first, n, k, eigs, status):
+            try:
+                a = np.ctypeslib.as_array(eigs, shape=(n * k,)).reshape(n, k).copy() if n else np.empty((0, k))
+                return int(write(req, seed_first, a, status) or 0)
+            except Exception:  # no exception may cross the C ABI
+                return JNE_ERR_IO
+
+        sink = Sink(SINK_WRITE(cb), None)
+        self._check(self._L.jne_run_batch_sink(self._h, arr, len(reqs), ctypes.byref(sink)))
+
+    def run_batch_to_dat(self, reqs: Sequence[dict], data_dir: str, finish: bool = True) -> None:
+        """The batch streamed by jne_dat_sink into each request's simulation file under data_dir."""
+        arr = self._requests(reqs)
+        sink = Sink()
+        _dat_check(self._L.jne_dat_sink_open(os.fsencode(data_dir), arr, len(reqs), ctypes.byref(sink)))
+        rc = self._L.jne_run_batch_sink(self._h, arr, len(reqs), ctypes.byref(sink))
+        rc2 = self._L.jne_dat_sink_close(ctypes.byref(sink), int(finish and rc == JNE_OK))
+        self._check(rc)
+        _dat_check(rc2)
 
     def plan(self, reqs: Sequence[dict], out_ptrs: Sequence[int]) -> "Plan":
         """jne_plan_create: the batch captured into a CUDA graph, replayed by Plan.launch()."""

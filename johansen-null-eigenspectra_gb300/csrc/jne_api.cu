@@ -75,6 +75,11 @@ void jne_close(jne_context* c) {
   if (c->ev_in) cudaEventDestroy(c->ev_in);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   for (int i = 0; i < 2; i++) {
+    cudaFree(c->d_sink[i]);
+    cudaFree(c->d_sink_st[i]);
+    cudaFreeHost(c->h_sink[i]);
+    cudaFreeHost(c->h_sink_st[i]);
+    if (c->ev_sink[i]) cudaEventDestroy(c->ev_sink[i]);
     cudaFree(c->d_reqs[i]);
     cudaFree(c->d_rtab[i]);
     cudaFree(c->d_counter[i]);

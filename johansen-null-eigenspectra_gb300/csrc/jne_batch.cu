@@ -259,6 +259,124 @@ int jne_run_batch_status(jne_context* c, const jne_request* reqs, int n_req, dou
   return JNE_OK;
 }
 
+namespace {
+
+// One round of a streamed batch in flight: its parts (request, first seed,
+// runs, offset of its results in the slot's buffers).
+struct SinkPart {
+  int req;
+  uint32_t seed_first;
+  int64_t n, off;
+};
+struct SinkRound {
+  std::vector<SinkPart> parts;
+  bool busy = false;
+};
+
+// Hands a finished round's results to the sink, in request order.
+int deliver(jne_context* c, const jne_request* reqs, const jne_sink* sink, int s, SinkRound& rd, int* worst) {
+  if (!rd.busy) return JNE_OK;
+  rd.busy = false;
+  cudaError_t e = cudaEventSynchronize(c->ev_sink[s]);
+  if (e != cudaSuccess) return cuda_fail(c, e, "sink round");
+  for (size_t p = 0; p < rd.parts.size(); p++) {
+    const SinkPart& q = rd.parts[p];
+    const int st = status_code(c->h_sink_st[s][p]);
+    if (st != JNE_OK && *worst == JNE_OK) *worst = st;
+    const int k = jne_eigen_count(reqs[q.req].model, reqs[q.req].dim);
+    const int rc = sink->write(sink->user, q.req, q.seed_first, q.n, k, c->h_sink[s] + q.off, st);
+    if (rc) return fail(c, rc, "the sink stopped the batch");
+  }
+  return JNE_OK;
+}
+
+}  // namespace
+
+int jne_run_batch_sink(jne_context* c, const jne_request* reqs, int n_req, const jne_sink* sink) {
+  if (!c) return JNE_ERR_ARG;
+  if (!sink || !sink->write || n_req < 0 || (n_req > 0 && !reqs)) return fail(c, JNE_ERR_ARG, "null sink or requests");
+  int rc;
+  for (int i = 0; i < n_req; i++) {
+    if ((rc = check_common(c, reqs[i].model, reqs[i].dim, reqs[i].steps, reqs[i].n_runs, reqs[i].precision)))
+      return rc;
+    if ((uint64_t)reqs[i].seed_first + (uint64_t)reqs[i].n_runs > 0x100000000ull)
+      return fail(c, JNE_ERR_ARG, "seed range exceeds u32");
+  }
+  // runs per round: 2^20, or what two slots of results fit in a sixteenth of the budget
+  const int64_t cap = std::max<int64_t>(
+      1, std::min<int64_t>(1 << 20, (int64_t)(c->budget / 16 / (2 * sizeof(double) * (JNE_MAX_DIM + 1)))));
+  for (int s = 0; s < 2; s++)
+    if (!c->ev_sink[s] && cudaEventCreateWithFlags(&c->ev_sink[s], cudaEventDisableTiming) != cudaSuccess)
+      return fail(c, JNE_ERR_CUDA, "sink events");
+  std::vector<int64_t> next((size_t)n_req, 0);
+  SinkRound rounds[2];
+  int s = 0, worst = JNE_OK;
+  rc = JNE_OK;
+  cudaStream_t st = c->stream;
+  for (;;) {
+    // the round: a slice of every request with runs left, in request order
+    std::vector<int> act;
+    for (int i = 0; i < n_req; i++)
+      if (next[(size_t)i] < reqs[i].n_runs) act.push_back(i);
+    if (act.empty()) break;
+    if ((rc = deliver(c, reqs, sink, s, rounds[s], &worst))) break;  // the slot's previous round
+    const int64_t share = std::max<int64_t>(1, cap / (int64_t)act.size());
+    SinkRound& rd = rounds[s];
+    rd.parts.clear();
+    std::vector<jne_request> sub;
+    int64_t doubles = 0;
+    for (int i : act) {
+      const int64_t n = std::min<int64_t>(share, reqs[i].n_runs - next[(size_t)i]);
+      jne_request r = reqs[i];
+      r.seed_first = reqs[i].seed_first + (uint32_t)next[(size_t)i];
+      r.n_runs = n;
+      sub.push_back(r);
+      rd.parts.push_back({i, r.seed_first, n, doubles});
+      doubles += n * jne_eigen_count(r.model, r.dim);
+      next[(size_t)i] += n;
+    }
+    const size_t np = rd.parts.size();
+    if ((rc = ensure(c, &c->d_sink[s], &c->d_sink_cap[s], (size_t)doubles, "sink results")) ||
+        (rc = ensure(c, &c->d_sink_st[s], &c->d_sink_st_cap[s], np, "sink status words")) ||
+        (rc = ensure_pinned(c, &c->h_sink[s], &c->h_sink_cap[s], (size_t)doubles)) ||
+        (rc = ensure_pinned(c, &c->h_sink_st[s], &c->h_sink_st_cap[s], np)))
+      break;
+    std::vector<double*> outs(np);
+    std::vector<unsigned int*> words(np);
+    for (size_t p = 0; p < np; p++) {
+      outs[p] = c->d_sink[s] + rd.parts[p].off;
+      words[p] = c->d_sink_st[s] + p;
+    }
+    cudaError_t e = cudaMemsetAsync(c->d_sink_st[s], 0, sizeof(unsigned int) * np, st);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(c, e, "sink status reset");
+      break;
+    }
+    if ((rc = run_batch(c, sub.data(), (int)np, outs.data(), st, words.data()))) break;
+    if ((e = cudaMemcpyAsync(c->h_sink[s], c->d_sink[s], sizeof(double) * doubles, cudaMemcpyDeviceToHost, st)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(c->h_sink_st[s], c->d_sink_st[s], sizeof(unsigned int) * np, cudaMemcpyDeviceToHost,
+                             st)) != cudaSuccess ||
+        (e = cudaEventRecord(c->ev_sink[s], st)) != cudaSuccess) {
+      rc = cuda_fail(c, e, "sink copy");
+      break;
+    }
+    rd.busy = true;
+    s ^= 1;
+  }
+  if (rc == JNE_OK) {  // the last two rounds, oldest first
+    rc = deliver(c, reqs, sink, s, rounds[s], &worst);
+    if (rc == JNE_OK) rc = deliver(c, reqs, sink, s ^ 1, rounds[s ^ 1], &worst);
+  }
+  if (rc) {
+    cudaStreamSynchronize(st);  // no round left writing into the slots
+    cudaStreamSynchronize(c->fin_stream);
+    return rc;
+  }
+  if (worst != JNE_OK) return fail(c, worst, "some runs of the batch had a non-SPD S11 (NaN rows delivered)");
+  return JNE_OK;
+}
+
 int jne_plan_create(jne_context* c, const jne_request* reqs, int n_req, double* const* outs, jne_plan** out) {
   if (!c) return JNE_ERR_ARG;
   if (!out || n_req < 1 || !reqs || !outs) return fail(c, JNE_ERR_ARG, "plans take a non-empty request list");

@@ -74,6 +74,16 @@ struct jne_context {
   size_t h_reqs_cap[2] = {0, 0};
   jne_chunk_time* h_rtab[2] = {nullptr, nullptr};
   size_t h_rtab_cap[2] = {0, 0};
+  // streaming sink: per round slot, device results and status words, pinned host copies
+  double* d_sink[2] = {nullptr, nullptr};
+  size_t d_sink_cap[2] = {0, 0};
+  unsigned int* d_sink_st[2] = {nullptr, nullptr};
+  size_t d_sink_st_cap[2] = {0, 0};
+  double* h_sink[2] = {nullptr, nullptr};
+  size_t h_sink_cap[2] = {0, 0};
+  unsigned int* h_sink_st[2] = {nullptr, nullptr};
+  size_t h_sink_st_cap[2] = {0, 0};
+  cudaEvent_t ev_sink[2] = {nullptr, nullptr};
   // per-kernel event timing (jne_profile)
   bool profiling = false;
   struct Timed {

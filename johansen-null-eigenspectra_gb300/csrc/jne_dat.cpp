@@ -439,6 +439,86 @@ int jne_dat_read(const char* path, int* model, int* dim, uint32_t* steps, int64_
   return JNE_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The .dat sink: one writer per distinct (model, dim, steps) file, and each
+// request's writer.
+struct DatSink {
+  std::vector<jne_dat_writer*> files;
+  std::vector<jne_dat_writer*> of_req;
+  std::vector<uint32_t> seeds;
+};
+
+int dat_sink_write(void* user, int req, uint32_t seed_first, int64_t n, int k, const double* eigs, int status) {
+  DatSink* d = static_cast<DatSink*>(user);
+  if (status != JNE_OK) return status;
+  d->seeds.resize((size_t)n);
+  for (int64_t r = 0; r < n; r++) d->seeds[(size_t)r] = seed_first + (uint32_t)r;
+  return jne_dat_append(d->of_req[(size_t)req], d->seeds.data(), eigs, n, k);
+}
+
+}  // namespace
+
+extern "C" {
+
+int jne_dat_sink_open(const char* data_dir, const jne_request* reqs, int n_req, jne_sink* out) {
+  if (!out || n_req < 0 || (n_req > 0 && !reqs)) return dat_fail(JNE_ERR_ARG, "null argument");
+  out->write = nullptr;
+  out->user = nullptr;
+  const std::string dir = data_dir && *data_dir ? data_dir : "data";
+  int rc = mkdirs(dir);
+  if (rc) return rc;
+  DatSink* d = new DatSink();
+  std::vector<std::string> names;
+  for (int i = 0; i < n_req && rc == JNE_OK; i++) {
+    char buf[4096];
+    if (jne_eigen_count(reqs[i].model, reqs[i].dim) < 0 || reqs[i].dim > JNE_MAX_DIM || reqs[i].steps < 1) {
+      rc = dat_fail(JNE_ERR_ARG, "bad request");
+      break;
+    }
+    if ((rc = jne_simulation_filename(dir.c_str(), reqs[i].model, reqs[i].dim, reqs[i].steps, buf, sizeof buf)))
+      break;
+    const auto it = std::find(names.begin(), names.end(), std::string(buf));
+    if (it != names.end()) {
+      d->of_req.push_back(d->files[(size_t)(it - names.begin())]);
+      continue;
+    }
+    jne_dat_writer* w = nullptr;
+    if ((rc = jne_dat_open(buf, reqs[i].model, reqs[i].dim, (uint32_t)reqs[i].steps, &w, nullptr))) break;
+    names.push_back(buf);
+    d->files.push_back(w);
+    d->of_req.push_back(w);
+  }
+  if (rc) {
+    for (jne_dat_writer* w : d->files) jne_dat_abandon(w);
+    delete d;
+    return rc;
+  }
+  out->write = dat_sink_write;
+  out->user = d;
+  return JNE_OK;
+}
+
+int jne_dat_sink_close(jne_sink* sink, int finish) {
+  if (!sink || !sink->user) return dat_fail(JNE_ERR_ARG, "null sink");
+  DatSink* d = static_cast<DatSink*>(sink->user);
+  int rc = JNE_OK;
+  for (jne_dat_writer* w : d->files) {
+    if (finish) {
+      const int r = jne_dat_finish(w);
+      if (r && rc == JNE_OK) rc = r;
+    } else {
+      jne_dat_abandon(w);
+    }
+  }
+  delete d;
+  sink->user = nullptr;
+  sink->write = nullptr;
+  return rc;
+}
+
 int jne_simulation_filename(const char* data_dir, int model, int dim, int steps, char* buf, size_t cap) {
   if (!buf || cap == 0) return dat_fail(JNE_ERR_ARG, "null buffer");
   const std::string dir = data_dir && *data_dir ? data_dir : "data";

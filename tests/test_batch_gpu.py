@@ -138,3 +138,77 @@ def test_results_visible_on_the_caller_stream_without_sync(engine, jne):
         for c, ref in zip(copies, refs):
             assert np.array_equal(c.cpu().numpy(), ref)
     engine.sync()
+
+
+def _collect_sink(eng, jne, reqs):
+    got = {i: [] for i in range(len(reqs))}
+    seeds = {i: [] for i in range(len(reqs))}
+    status = {i: [] for i in range(len(reqs))}
+
+    def write(req, seed_first, eigs, st):
+        got[req].append(eigs)
+        seeds[req].append((seed_first, eigs.shape[0]))
+        status[req].append(st)
+        return 0
+
+    return got, seeds, status, write
+
+
+def test_sink_streams_each_request_in_seed_order(jne):
+    """Under a small budget every request spans several rounds: each request's results arrive in seed order,
+    contiguous, and equal its single-request results bit for bit (ragged, FP64 and short requests)."""
+    reqs = [dict(model=0, dim=2, steps=500, n_runs=50_000), MIX[1], MIX[5], MIX[6], MIX[7],
+            dict(model=3, dim=12, steps=1000, n_runs=30_000, seed_first=4)]
+    with jne.Engine(0, mem_budget_bytes=64 << 20) as small, jne.Engine(0) as ref_eng:
+        got, seeds, status, write = _collect_sink(small, jne, reqs)
+        small.run_batch_sink(reqs, write)
+        assert len(seeds[0]) > 1 and len(seeds[5]) > 1  # several rounds
+        for i, r in enumerate(reqs):
+            s0 = r.get("seed_first", 1)
+            pos = s0
+            for first, n in seeds[i]:
+                assert first == pos
+                pos += n
+            assert pos == s0 + r["n_runs"]
+            assert all(st == jne.JNE_OK for st in status[i])
+            res = np.concatenate(got[i]) if got[i] else np.empty((0, jne.eigen_count(r["model"], r["dim"])))
+            assert np.array_equal(res, _single(ref_eng, jne, r)), r
+
+
+def test_sink_reports_a_singular_request_and_can_stop_the_batch(engine, jne):
+    reqs = [MIX[0], dict(model=0, dim=3, steps=1, n_runs=5), MIX[2]]
+    got, seeds, status, write = _collect_sink(engine, jne, reqs)
+    with pytest.raises(jne.JneError) as ei:
+        engine.run_batch_sink(reqs, write)
+    assert ei.value.code == jne.JNE_ERR_NUMERIC  # after every result was delivered
+    assert status[1] == [jne.JNE_ERR_NUMERIC] and np.isnan(got[1][0]).all()
+    assert status[0] == [jne.JNE_OK] and status[2] == [jne.JNE_OK]
+    assert np.array_equal(got[0][0], _single(engine, jne, reqs[0]))
+    calls = []
+
+    def stop(req, seed_first, eigs, st):
+        calls.append(req)
+        return 7  # any non-zero status stops the batch
+
+    with pytest.raises(jne.JneError) as ei:
+        engine.run_batch_sink([MIX[0], MIX[2]], stop)
+    assert ei.value.code == 7 and calls == [0]
+    engine.sync()
+
+
+def test_dat_sink_writes_the_simulation_files(engine, jne, tmp_path):
+    """jne_dat_sink: every request's records appended to its simulation file (the reference's name); two
+    requests of the same (model, dim, steps) share a file; the trailer is written at close."""
+    reqs = [dict(model=1, dim=3, steps=400, n_runs=700), dict(model=4, dim=9, steps=600, n_runs=90, precision=0),
+            dict(model=1, dim=3, steps=400, n_runs=300, seed_first=701)]
+    engine.run_batch_to_dat(reqs, str(tmp_path))
+    recs, model, dim, steps = jne.read_dat(str(tmp_path / "eigenvalues_model1_dim3_steps400.dat"))
+    assert (model, dim, steps) == (1, 3, 400)
+    assert list(recs.seeds) == list(range(1, 1001))
+    whole = engine.eigs_seeded(1, 3, 400, 1, 1000, precision=jne.PREC_MIXED)
+    assert np.array_equal(recs.eigs, whole)
+    recs, model, dim, steps = jne.read_dat(str(tmp_path / "eigenvalues_model4_dim9_steps600.dat"))
+    assert list(recs.seeds) == list(range(1, 91))
+    assert np.array_equal(recs.eigs, engine.eigs_seeded(4, 9, 600, 1, 90, precision=0))
+    raw = open(tmp_path / "eigenvalues_model4_dim9_steps600.dat", "rb").read()
+    assert raw[-17:-9] == b"EOF_MARK"
