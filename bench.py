@@ -39,13 +39,13 @@ UNIT = "runs/s"
 
 # DRAM bytes (read + write) of one k_accum_mixed<12> launch (accumulation + fused
 # finalize) per run, from an ncu capture of the full 200,000-run launch
-# (profiles/k_accum_mixed_dim12_T10k_dram.md): 24,073,472 B read + 965,540,864 B written.
+# (profiles/k_accum_mixed_dim12_T10k_dram.md): 22,712,064 B read + 779,393,024 B written.
 # Algorithmic: 2,352 B of record written and read back, 96 B of eigenvalues per run.
-ACCUM_DRAM_BYTES_PER_RUN = (24_073_472 + 965_540_864) / 200_000
+ACCUM_DRAM_BYTES_PER_RUN = (22_712_064 + 779_393_024) / 200_000
 # Warp instructions k_accum_mixed<12> issues per run at T = 10,000 (accumulation plus
 # the run's share of its fused finalize batch), from an ncu capture of an 8,192-run
-# launch (profiles/k_accum_mixed_dim12_T10k_8192runs_full.md).
-ACCUM_WARP_INST_PER_RUN = 174_587
+# launch (profiles/k_accum_mixed_dim12_T10k_8192runs_full.md): 1,267,252,196 / 8,192.
+ACCUM_WARP_INST_PER_RUN = 154_694
 
 
 def k_of(model: int) -> int:
@@ -319,7 +319,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "frac": (achieved / bf16) if bf16 else None, "traffic": traffic,
             "traffic_note": "ncu dram bytes of one full 200k-run launch (accumulation + fused finalize), per "
                             "run x runs per launch; algorithmic: 2,352 B/run of records, 96 B/run of eigenvalues",
-            "kernel": "k_accum_mixed<12,false>", "peak_source": "measured bf16_tflops (burst)" if bf16 else "none",
+            "kernel": "k_accum_mixed<12,false,4,true>", "peak_source": "measured bf16_tflops (burst)" if bf16 else "none",
             "flops_per_run": W}
     normals_rate = DIM * STEPS * R / (mean_acc_ms * 1e-3)
     rates = eng.probe_rates()
