@@ -356,14 +356,18 @@ def run_gpu(args, rank: int, world: int) -> None:
                     if args.tune_err > 0 and rank == 0 else None)
     # all five models of the same seeds from one pass over the paths (jne_eigs_seeded_models): the path of a
     # seed does not depend on the model, so one accumulation serves five finalizes; host outputs
-    eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, min(R, 20_000), precision=jne.PREC_MIXED)
+    eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, R, precision=jne.PREC_MIXED)  # warm, full size
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, R, precision=jne.PREC_MIXED)
-    one_pass_s = time.perf_counter() - t0
+    walls = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        eng.eigs_seeded_models(list(MODELS), DIM, STEPS, seed0, R, precision=jne.PREC_MIXED)
+        walls.append(time.perf_counter() - t0)
+    one_pass_s = min(walls)
     one_pass = {"runs_per_s": len(MODELS) * R / one_pass_s, "seconds": one_pass_s,
                 "workload": f"models 0-4 x {R} seeds, dim {DIM}, T {STEPS}, mixed, one accumulation per seed "
-                            "(jne_eigs_seeded_models), eigenvalues copied to host memory; wall clock",
+                            "(jne_eigs_seeded_models), eigenvalues copied to host memory; wall clock, the faster "
+                            "of two calls after a full-size warm-up",
                 "note": "not the headline: the headline runs one request per model, as the reference does"}
     serving = None
     if rank == 0 and (args.serve_seconds > 0 or args.serve_low_seconds > 0):
