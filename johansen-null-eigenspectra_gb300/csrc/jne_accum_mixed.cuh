@@ -240,10 +240,9 @@ struct Packing {
 // run r (packed); rows without a feature are zero.  See the file comment for
 // the lane <-> (row, step) mapping.
 template <int DIM, bool EXT, bool FULL, bool PACK>
-__device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, int tloc, int nvalid,
-                                          float invL, const float (&cA)[4], const float (&cB)[4],
-                                          float& chiA, float& cloA, float& chiB, float& cloB, float (&acc)[3][4],
-                                          float (&accx)[3][4]) {
+__device__ __forceinline__ void tile_body(const float (*zs)[kZS], const float (*bw)[32], int g, int q, int nvalid,
+                                          float cA0, float cB0, int selA, int selB, float& chiA, float& cloA,
+                                          float& chiB, float& cloB, float (&acc)[3][4], float (&accx)[3][4]) {
   // Unpacked: zA = increments of row g; zB = of row 8 + (g & 3) -- the walk of
   // row g + 8 for g < 4, the B operand of Gram block 1 for g >= 4.  Packed:
   // zA = run A's feature g for g < 4, run B's feature g - 4 for g >= 4 (the B
@@ -264,9 +263,16 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
       for (int j = 0; j < 8; j++) zB[j] = 0.f;
     }
   }
-  // lane totals and the exclusive scan over the 4 lanes of the group
-  float tA = ((zA[0] + zA[1]) + (zA[2] + zA[3])) + ((zA[4] + zA[5]) + (zA[6] + zA[7]));
-  float tB = ((zB[0] + zB[1]) + (zB[2] + zB[3])) + ((zB[4] + zB[5]) + (zB[6] + zB[7]));
+  // lane-local exclusive prefixes pre[j] = z[0] + ... + z[j-1], the lane totals, and the exclusive scan of
+  // the totals over the 4 lanes of the group
+  float preA[8], preB[8];
+  preA[0] = 0.f; preB[0] = 0.f; preA[1] = zA[0]; preB[1] = zB[0];
+#pragma unroll
+  for (int j = 2; j < 8; j++) {
+    preA[j] = preA[j - 1] + zA[j - 1];
+    preB[j] = preB[j - 1] + zB[j - 1];
+  }
+  float tA = preA[7] + zA[7], tB = preB[7] + zB[7];
   float xA = tA, xB = tB;
   {
     float yA = __shfl_up_sync(0xffffffffu, xA, 1, 4), yB = __shfl_up_sync(0xffffffffu, xB, 1, 4);
@@ -279,30 +285,28 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
   if (q == 0) { eA = 0.f; eB = 0.f; }
   const float tileA = __shfl_sync(0xffffffffu, xA, 3, 4), tileB = __shfl_sync(0xffffffffu, xB, 3, 4);
 
-  // G rows rA = g and rB = g + 8 at the lane's 8 steps
+  // G rows rA = g and rB = g + 8 at the lane's 8 steps: walk rows c0 = 1 plus a zero basis value, basis rows
+  // c0 = 0 plus their value (1, u or u^2) at the step, from the window the producer filled
   float GA[8], GB[8];
-  float pA = cloA + eA, pB = cloB + eB;  // tile-local walk (+ carry low word)
-  const float u0 = (float)tloc * invL;
-  // P(u) = c1 + c2 u + c3 u^2 at u0 + j h by forward differences
-  float PA = fmaf(fmaf(cA[3], u0, cA[2]), u0, cA[1]), PB = fmaf(fmaf(cB[3], u0, cB[2]), u0, cB[1]);
-  const float h = invL, h2 = invL * invL;
-  float DA = fmaf(cA[3], fmaf(2.0f * u0, h, h2), cA[2] * h), DB = fmaf(cB[3], fmaf(2.0f * u0, h, h2), cB[2] * h);
-  const float D2A = 2.0f * cA[3] * h2, D2B = 2.0f * cB[3] * h2;
+  // the walk at the lane's first step: carry (hi + lo) + the group's exclusive prefix, folded into one float
+  const float wA = chiA + (cloA + eA), wB = chiB + (cloB + eB);
+  constexpr bool A_WALK_ONLY = DIM >= 8 && !PAIR;  // rows 0..7 are all walk rows
+  float vA[8], vB[8];
+  {
+    const float4 b0 = *reinterpret_cast<const float4*>(&bw[selB][8 * q]);
+    const float4 b1 = *reinterpret_cast<const float4*>(&bw[selB][8 * q + 4]);
+    vB[0] = b0.x; vB[1] = b0.y; vB[2] = b0.z; vB[3] = b0.w; vB[4] = b1.x; vB[5] = b1.y; vB[6] = b1.z; vB[7] = b1.w;
+    if (!A_WALK_ONLY) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&bw[selA][8 * q]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&bw[selA][8 * q + 4]);
+      vA[0] = a0.x; vA[1] = a0.y; vA[2] = a0.z; vA[3] = a0.w; vA[4] = a1.x; vA[5] = a1.y; vA[6] = a1.z; vA[7] = a1.w;
+    }
+  }
 #pragma unroll
   for (int j = 0; j < 8; j++) {
-    const float bA = chiA + pA, bB = chiB + pB;
-    pA += zA[j];
-    pB += zB[j];
-    if (DIM >= 8) {
-      GA[j] = bA;
-    } else {
-      GA[j] = fmaf(cA[0], bA, PA);
-      PA += DA;
-      DA += D2A;
-    }
-    GB[j] = fmaf(cB[0], bB, PB);
-    PB += DB;
-    DB += D2B;
+    const float bA = j == 0 ? wA : wA + preA[j], bB = j == 0 ? wB : wB + preB[j];
+    GA[j] = A_WALK_ONLY ? bA : fmaf(cA0, bA, vA[j]);
+    GB[j] = fmaf(cB0, bB, vB[j]);
     if (!FULL) {
       if (8 * q + j >= nvalid) { GA[j] = 0.f; GB[j] = 0.f; }
     }
@@ -390,6 +394,7 @@ __device__ __forceinline__ void tile_body(const float (*zs)[kZS], int g, int q, 
 constexpr int kRecMax = JNE_MAX_DIM * (JNE_MAX_DIM + 1) / 2 + 6 * JNE_MAX_DIM + JNE_MAX_DIM * JNE_MAX_DIM;
 struct alignas(16) WarpSmem {
   float zs[16][kZS];      // increments of the current tile: z[feature][step]
+  float bw[4][32];        // basis rows at the current tile's steps: 0, 1, u, u^2
   float cm[16][kCS];      // the chunk's local Gram, staged for the merge
   // float-float values are (hi, lo) pairs
   float2 wc[16];           // walk at the chunk start
@@ -451,18 +456,14 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
   }
   // G-row coefficients: value = c[0]*b + c[1] + c[2]*u + c[3]*u^2 (packed: the
   // lane's rows g and g + 8 are local row g of runs A and B)
-  float cA[4], cB[4];
-  {
-    const int r[2] = {g, PAIR ? g : g + 8};
-    for (int h = 0; h < 2; h++) {
-      float* cc = h ? cB : cA;
-      const int rr = r[h];
-      cc[0] = rr < d ? 1.f : 0.f;
-      cc[1] = rr == d ? 1.f : 0.f;
-      cc[2] = rr == d + 1 ? 1.f : 0.f;
-      cc[3] = rr == d + 2 ? 1.f : 0.f;
-    }
-  }
+  // the lane's rows: walk rows take c0 = 1 and the zero basis row (0); the basis rows take c0 = 0 and the
+  // window row of their value: 1 (1), u (2), u^2 (3)
+  const int rowA = g, rowB = PAIR ? g : g + 8;
+  const float cA0 = rowA < d ? 1.f : 0.f, cB0 = rowB < d ? 1.f : 0.f;
+  const int selA = rowA == d ? 1 : rowA == d + 1 ? 2 : rowA == d + 2 ? 3 : 0;
+  const int selB = rowB == d ? 1 : rowB == d + 1 ? 2 : rowB == d + 2 ? 3 : 0;
+  sm.bw[0][lane] = 0.f;
+  sm.bw[1][lane] = 1.f;
   const int T = a.steps, L = a.chunk;
   const float invL = 1.0f / (float)L;
   const float invTf = 1.0f / (float)T;
@@ -513,13 +514,19 @@ __device__ __forceinline__ void accum_unit(const jne_accum_args& a, int unit, Wa
             for (int f = 0; f < d; f++) zs[row0 + f][lane] = 0.f;
         }
       }
+      {  // the basis rows at this tile's steps: u = (step - chunk start) / L
+        const float u = __fmul_rn((float)(i - c0), invL);
+        sm.bw[2][lane] = u;
+        sm.bw[3][lane] = __fmul_rn(u, u);
+      }
       __syncwarp();
       const int nvalid = min(32, T - t0);
-      const int tloc = t0 - c0 + 8 * q;
       if (nvalid == 32)
-        tile_body<DIM, EXT, true, PACK>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
+        tile_body<DIM, EXT, true, PACK>(zs, sm.bw, g, q, nvalid, cA0, cB0, selA, selB, chiA, cloA, chiB, cloB, acc,
+                                        accx);
       else
-        tile_body<DIM, EXT, false, PACK>(zs, g, q, tloc, nvalid, invL, cA, cB, chiA, cloA, chiB, cloB, acc, accx);
+        tile_body<DIM, EXT, false, PACK>(zs, sm.bw, g, q, nvalid, cA0, cB0, selA, selB, chiA, cloA, chiB, cloB, acc,
+                                         accx);
       __syncwarp();
     }
 
