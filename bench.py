@@ -39,13 +39,13 @@ UNIT = "runs/s"
 
 # DRAM bytes (read + write) of one k_accum_mixed<12> launch (accumulation + fused
 # finalize) per run, from an ncu capture of the full 200,000-run launch
-# (profiles/k_accum_mixed_dim12_T10k_dram.md): 22,712,064 B read + 779,393,024 B written.
+# (profiles/k_accum_mixed_dim12_T10k_dram.md): 18,147,072 B read + 771,372,800 B written.
 # Algorithmic: 2,352 B of record written and read back, 96 B of eigenvalues per run.
-ACCUM_DRAM_BYTES_PER_RUN = (22_712_064 + 779_393_024) / 200_000
+ACCUM_DRAM_BYTES_PER_RUN = (18_147_072 + 771_372_800) / 200_000
 # Warp instructions k_accum_mixed<12> issues per run at T = 10,000 (accumulation plus
 # the run's share of its fused finalize batch), from an ncu capture of an 8,192-run
-# launch (profiles/k_accum_mixed_dim12_T10k_8192runs_full.md): 1,267,252,196 / 8,192.
-ACCUM_WARP_INST_PER_RUN = 154_694
+# launch (profiles/k_accum_mixed_dim12_T10k_8192runs_full.md): 1,166,615,378 / 8,192.
+ACCUM_WARP_INST_PER_RUN = 142_409
 
 
 def k_of(model: int) -> int:
