@@ -226,3 +226,38 @@ def test_short_write_leaves_whole_records(jne, tmp):
     seeds = np.asarray(recs.seeds, dtype=np.int64)
     seed_bytes = 1 + (seeds >= 1 << 7) + (seeds >= 1 << 14) + (seeds >= 1 << 21)
     assert size == 18 + int(np.sum(seed_bytes + 17))
+
+
+def test_dat_sink_host_side(jne, tmp):
+    """jne_dat_sink_open/close and its write callback, driven directly (no GPU): records reach each
+    request's simulation file in the order written, requests of the same (model, dim, steps) share a file,
+    a non-OK status stops with that status, and close writes the trailers."""
+    import ctypes
+
+    L = jne.lib()
+    reqs = (jne.Request * 3)(jne.Request(0, 2, 100, 1, 7, 1, 4), jne.Request(3, 2, 50, 1, 7, 1, 3),
+                             jne.Request(0, 2, 100, 1, 7, 5, 2))
+    sink = jne.Sink()
+    assert L.jne_dat_sink_open(os.fsencode(tmp), reqs, 3, ctypes.byref(sink)) == jne.JNE_OK
+
+    def write(req, seed_first, eigs, status=jne.JNE_OK):
+        e = np.ascontiguousarray(eigs, dtype=np.float64)
+        return sink.write(sink.user, req, seed_first, e.shape[0], e.shape[1],
+                          e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), status)
+
+    a = np.arange(8.0).reshape(4, 2)
+    b = np.arange(9.0).reshape(3, 3) + 100
+    c = np.arange(4.0).reshape(2, 2) + 50
+    assert write(0, 1, a[:3]) == jne.JNE_OK
+    assert write(1, 1, b) == jne.JNE_OK
+    assert write(0, 4, a[3:]) == jne.JNE_OK
+    assert write(2, 5, c) == jne.JNE_OK
+    assert write(2, 7, c[:1], jne.JNE_ERR_NUMERIC) == jne.JNE_ERR_NUMERIC  # NaN rows are not written
+    assert L.jne_dat_sink_close(ctypes.byref(sink), 1) == jne.JNE_OK
+    recs, model, dim, steps = jne.read_dat(os.path.join(tmp, "eigenvalues_model0_dim2_steps100.dat"))
+    assert (model, dim, steps) == (0, 2, 100)
+    assert list(recs.seeds) == [1, 2, 3, 4, 5, 6]
+    assert np.array_equal(recs.eigs, np.vstack([a, c]))
+    recs, model, dim, steps = jne.read_dat(os.path.join(tmp, "eigenvalues_model3_dim2_steps50.dat"))
+    assert list(recs.seeds) == [1, 2, 3] and np.array_equal(recs.eigs, b)
+    assert open(os.path.join(tmp, "eigenvalues_model3_dim2_steps50.dat"), "rb").read()[-17:-9] == b"EOF_MARK"
