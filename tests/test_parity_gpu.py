@@ -231,3 +231,18 @@ def test_longest_chunk_keeps_fp16_operands_finite(jne):
             f = eng.eigs_seeded(0, dim, 16384, 1, 64, precision=0)
             assert np.all(np.isfinite(m))
             assert normwise_err(m, f, 1.0) < 1e-3, dim
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_every_dim_and_model_vs_oracle(engine, oracle, precision):
+    """dims 1..12 x models 0..4 at T = 3000 (chunk 128: several chunks and a partial last tile), 4 runs each,
+    against the oracle on the kernels' own increments; mixed also against its max-eig / trace bound."""
+    steps = 3000
+    for dim in range(1, 13):
+        dB, _ = engine.export_increments(dim, steps, 21, 4)
+        for model in range(5):
+            ref = oracle.c_eigs_from_increments(model, dB)
+            got = engine.eigs_seeded(model, dim, steps, 21, 4, precision=precision)
+            assert normwise_err(got, ref, FLOOR[precision]) < tol(precision, steps), (model, dim)
+            if precision == 1:
+                assert np.max(np.abs(got[:, 0] - ref[:, 0]) / np.maximum(ref[:, 0], 1.0)) <= 1e-6, (model, dim)
