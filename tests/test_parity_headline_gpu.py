@@ -5,7 +5,7 @@ The kernels against the CPU oracle (not against each other):
 * per run, on the increments the kernels draw (exported through the C ABI and
   walked by the oracle's dense restatement of johansen_statistics.rs:59-85):
   plain FP64 within 1e-9 normwise-relative; mixed precision within 1e-6
-  relative on the largest eigenvalue and on the trace, and 2e-6 normwise
+  relative on the largest eigenvalue and on the trace, and 1e-6 normwise
   (relative to max(lambda_max, 1));
 * on the dggev golden fixture at this shape (explicit increments);
 * in distribution: 5,000 GPU runs per model and precision against 5,000 runs of
@@ -28,7 +28,7 @@ pytestmark = pytest.mark.gpu
 DIM, STEPS = 12, 10_000
 TOL_FP64 = 1e-9
 TOL_MIXED_STAT = 1e-6  # max-eig and trace, relative
-TOL_MIXED_NORMWISE = 2e-6
+TOL_MIXED_NORMWISE = 1e-6  # every eigenvalue, relative to max(lambda_max, 1): the stated 1e-6 target
 PS = (0.01, 0.05, 0.1, 0.5, 0.9, 0.95, 0.99)
 
 
