@@ -246,3 +246,31 @@ def test_every_dim_and_model_vs_oracle(engine, oracle, precision):
             assert normwise_err(got, ref, FLOOR[precision]) < tol(precision, steps), (model, dim)
             if precision == 1:
                 assert np.max(np.abs(got[:, 0] - ref[:, 0]) / np.maximum(ref[:, 0], 1.0)) <= 1e-6, (model, dim)
+
+
+def test_long_paths_vs_oracle(engine, oracle):
+    """T = 50,000 (98 chunks of 512 steps in mixed precision), dims 4 and 12, all five models, against the
+    oracle on the kernels' own increments: FP64 1e-9, mixed 2e-6 normwise and 1e-6 on the largest eigenvalue."""
+    steps = 50_000
+    for dim in (4, 12):
+        dB, _ = engine.export_increments(dim, steps, 7, 3)
+        for model in range(5):
+            ref = oracle.c_eigs_from_increments(model, dB, n_threads=3)
+            f64 = engine.eigs_seeded(model, dim, steps, 7, 3, precision=0)
+            mix = engine.eigs_seeded(model, dim, steps, 7, 3, precision=1)
+            assert normwise_err(f64, ref) < TOL_FP64, (model, dim)
+            assert normwise_err(mix, ref, 1.0) < TOL_MIXED, (model, dim)
+            assert np.max(np.abs(mix[:, 0] - ref[:, 0]) / ref[:, 0]) <= 1e-6, (model, dim)
+
+
+def test_seeds_at_the_top_of_the_u32_range(engine, oracle):
+    """The last seeds a request may name (seed_first + n_runs - 1 = 2^32 - 1): Philox words bit-exact with the
+    oracle, eigenvalues within the FP64 tolerance on the kernels' own increments."""
+    first, n, dim, steps = 2**32 - 5, 5, 6, 400
+    dB, words = engine.export_increments(dim, steps, first, n, words=True)
+    for r in range(n):
+        assert np.array_equal(words[r], oracle.c_philox_words(oracle.DEFAULT_BASE_SEED, dim, first + r, steps))
+    for model in (0, 3):
+        ref = oracle.c_eigs_from_increments(model, dB)
+        assert normwise_err(engine.eigs_seeded(model, dim, steps, first, n, precision=0), ref) < TOL_FP64
+        assert normwise_err(engine.eigs_seeded(model, dim, steps, first, n, precision=1), ref, 1.0) < TOL_MIXED
