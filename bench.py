@@ -369,6 +369,7 @@ def run_gpu(args, rank: int, world: int) -> None:
                             "(jne_eigs_seeded_models), eigenvalues copied to host memory; wall clock, the faster "
                             "of two calls after a full-size warm-up",
                 "note": "not the headline: the headline runs one request per model, as the reference does"}
+    packer = bench_record_packer(jne, torch, eng, args.pack_records) if args.pack_records > 0 and rank == 0 else None
     serving = None
     if rank == 0 and (args.serve_seconds > 0 or args.serve_low_seconds > 0):
         serving = {}
@@ -415,6 +416,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "gpu_launches": acc_n + fin_n,
             "roofline": roof, "issue_bound": issue, "kernel_ms": kern,
             "ragged60": ragged, "ragged60_tuned": ragged_tuned, "tuned_single": tuned_single, "serving": serving, "precision_model4": precision, "models_one_pass": one_pass,
+            "record_packer": packer,
             "cpu_baseline": cpu, "clocks": clocks,
         }))
     eng.close()
@@ -561,6 +563,53 @@ def precision_vs_oracle(jne, local: int, oracle, runs: int, threads: int) -> dic
             "oracle": "C restatement of the dense reference algorithm on the kernels' own increments"}
 
 
+def bench_record_packer(jne, torch, eng, n: int, k: int = 13, reps: int = 10) -> dict:
+    """The .dat sink's device record packer on one sink round's worth of results (n records of k values,
+    seeds 1..n), timed with CUDA events on its launching stream, against the measured HBM copy bandwidth;
+    beside it the host encoder (jne_dat_append) writing the same records to a file."""
+    import tempfile
+
+    nbytes = jne.record_bytes(1, n, k)
+    eigs = torch.randn((n, k), dtype=torch.float64, device="cuda")
+    buf = torch.empty(nbytes + 16, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
+
+    def launch():
+        eng.pack_records_device(1, n, k, eigs.data_ptr(), buf.data_ptr(), nbytes + 16, stream=st.cuda_stream)
+
+    for _ in range(3):
+        launch()
+    st.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        launch()
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    moved = 8 * n * k + nbytes  # values read + records written
+    hbm = measured_peaks().get("hbm_gbs")
+    gbs = moved / (ms * 1e-3) / 1e9
+    host = eigs.cpu().numpy()
+    seeds = np.arange(1, n + 1, dtype=np.uint32)
+    with tempfile.TemporaryDirectory() as d:
+        w = jne.DatWriter(os.path.join(d, "enc.dat"), 1, k - 1, 100)  # model 1: k = dim + 1
+        t0 = time.perf_counter()
+        w.append(seeds, host)
+        host_s = time.perf_counter() - t0
+        w.abandon()
+    return {"records": n, "values_per_record": k, "bytes": nbytes, "ms_per_launch": ms,
+            "records_per_s": n / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": gbs / hbm if hbm else None, "algorithmic_bytes": moved,
+                         "peak_source": "measured hbm_gbs" if hbm else "none"},
+            "host_encode_records_per_s": n / host_s,
+            "workload": f"{n} records of {k} f64 (seeds 1..{n}, 1-3 byte ULEB128 seeds) packed on the GPU "
+                        f"(k_pack_records, mean of {reps} launches, inputs and output {moved / 1e6:.0f} MB > L2); "
+                        "host line: jne_dat_append of the same records into a file (wall clock)"}
+
+
 def bench_serving(jne, local: int, seconds: float, rate: float = 200.0, seed: int = 0xC5) -> dict:
     """Poisson arrivals (mean `rate` req/s) for `seconds`; model U{0..4}, dim U{1..12}, T log-U[500, 2e4],
     runs log-U[1e3, 1e6], per-request seed; 40 GB budget.  Latency = finish - submit, split into queueing
@@ -650,6 +699,8 @@ def main() -> None:
                     help="runs of the model-4 precision line also checked against the CPU oracle (0: skip)")
     ap.add_argument("--c3-runs", type=int, default=10_000_000,
                     help="model-4 precision run: mixed runs (error on the first 10,000 vs FP64; 0: skip)")
+    ap.add_argument("--pack-records", type=int, default=1 << 20,
+                    help="records of the device record packer line (0: skip)")
     ap.add_argument("--rng-peak", type=float, default=None,
                     help="Philox+Box-Muller normals/s (default: measured live by jne_probe_rates)")
     args = ap.parse_args()

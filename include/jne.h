@@ -21,6 +21,8 @@
  *                              models, src/main.rs:109-114)
  *   jne_export_increments      src/rng_matrix.rs:57-141 (the path itself)
  *   jne_dat_*                  src/data_storage/{writer,reader,uleb128}.rs
+ *   jne_record_bytes,          the record encoding of writer.rs:206-259 and
+ *   jne_pack_records_device    uleb128.rs:68-87, on the GPU
  *   jne_simulation_*           src/data_storage/simulation.rs:25-122 and
  *                              parallel_compute.rs:150-232
  *   jne_percentiles(_device)   src/simulation_analyzers.rs:4-81
@@ -213,12 +215,21 @@ typedef struct jne_sink {
    * jne_run_batch_sink returns it. */
   int (*write)(void* user, int req, uint32_t seed_first, int64_t n, int k, const double* eigs, int status);
   void* user;
+  /* Optional (null: unused).  When set, the batch packs each slice of results
+   * into .dat records on the GPU (jne_pack_records_device) and hands over their
+   * bytes instead of the eigenvalues: n_bytes = jne_record_bytes(seed_first, n,
+   * k) bytes in host memory, valid during the call, that jne_dat_append_packed
+   * appends as they are.  `write` is then not called and may be null.  The
+   * record stream replaces writer.rs:206-259's per-record encoding. */
+  int (*write_records)(void* user, int req, uint32_t seed_first, int64_t n, int k, const unsigned char* records,
+                       int64_t n_bytes, int status);
 } jne_sink;
 
 /* The batch of jne_run_batch, streamed to `sink`.  Synchronous: returns when
  * every result has been delivered (JNE_OK, or JNE_ERR_NUMERIC when some rows
  * were NaN), when the sink stops it (its code), or on an error.  Rounds hold up
- * to 2^20 runs (fewer under a small budget). */
+ * to 2^20 runs (fewer under a small budget).  The sink needs write or
+ * write_records; with write_records the records are packed on the GPU. */
 int jne_run_batch_sink(jne_context* ctx, const jne_request* reqs, int n_req, const jne_sink* sink);
 
 /* A sink that appends each request's records to its simulation file
@@ -226,8 +237,10 @@ int jne_run_batch_sink(jne_context* ctx, const jne_request* reqs, int n_req, con
  * "data", created on demand; requests with the same (model, dim, steps) share
  * the file; an existing file is appended to as jne_dat_open does).  Results
  * with a non-OK status stop the batch with that status (the reference's writer
- * never sees such a run: its sort panics first).  jne_dat_sink_close writes the
- * EOF trailers (finish != 0) or leaves the files as an interrupted run does. */
+ * never sees such a run: its sort panics first).  It sets both callbacks, so
+ * jne_run_batch_sink packs the records on the GPU (clear write_records to have
+ * them encoded on the host instead: the same bytes).  jne_dat_sink_close writes
+ * the EOF trailers (finish != 0) or leaves the files as an interrupted run does. */
 int jne_dat_sink_open(const char* data_dir, const jne_request* reqs, int n_req, jne_sink* out);
 int jne_dat_sink_close(jne_sink* sink, int finish);
 
@@ -315,6 +328,25 @@ int jne_dat_open(const char* path, int model, int dim, uint32_t steps, jne_dat_w
 /* Appends n records (seeds[r], eigs[r*k .. r*k+k-1]) (writer.rs:206-259): k <= 255
  * and the same for every record of the file, else JNE_ERR_FORMAT. */
 int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs, int64_t n, int k);
+
+/* Bytes of the records of n consecutive seeds seed_first .. seed_first + n - 1
+ * with k values each, in the record format above (ULEB128 seed, u8 count, k x
+ * f64 LE; uleb128.rs:68-87, writer.rs:242-249); -1 when n < 0, k is outside
+ * 0..255 or the seeds leave u32. */
+int64_t jne_record_bytes(uint32_t seed_first, int64_t n, int k);
+
+/* The records of n results of consecutive seeds seed_first.. (eigs_device:
+ * n x k f64 in device memory, run-major) packed on the GPU into out_device
+ * (device memory, 16-byte aligned, cap >= jne_record_bytes bytes).  Enqueued on
+ * `stream` (null: the context's stream); asynchronous.  The bytes are those
+ * jne_dat_append writes for the same records. */
+int jne_pack_records_device(jne_context* ctx, uint32_t seed_first, int64_t n, int k, const double* eigs_device,
+                            unsigned char* out_device, int64_t cap, void* stream);
+
+/* Appends n records of consecutive seeds seed_first.. already packed
+ * (jne_record_bytes(seed_first, n, k) bytes, host memory), with the checks and
+ * the short-write handling of jne_dat_append. */
+int jne_dat_append_packed(jne_dat_writer* w, uint32_t seed_first, int64_t n, int k, const unsigned char* records);
 
 /* Writes the EOF trailer (count, eigenvalues per record) and closes (writer.rs:262-302). */
 int jne_dat_finish(jne_dat_writer* w);

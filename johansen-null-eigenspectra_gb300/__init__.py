@@ -33,7 +33,8 @@ EXPORTS = (
     "jne_eigs_from_increments", "jne_eigs_seeded", "jne_eigs_seeded_device", "jne_eigs_seeded_models",
     "jne_export_increments", "jne_profile", "jne_profile_read", "jne_probe_rates", "jne_sync", "jne_autotune_chunk",
     "jne_autotune", "jne_set_launch_shape",
-    "jne_dat_open", "jne_dat_append", "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
+    "jne_dat_open", "jne_dat_append", "jne_dat_append_packed", "jne_record_bytes", "jne_pack_records_device",
+    "jne_dat_finish", "jne_dat_abandon", "jne_dat_read", "jne_dat_last_error",
     "jne_simulation_filename", "jne_simulation_run", "jne_simulation_run_models", "jne_percentiles",
     "jne_percentiles_device",
     "jne_eigs_seeded_noalloc", "jne_noalloc_last_error",
@@ -66,10 +67,15 @@ SINK_WRITE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctype
                               ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int)
 
 
-class Sink(ctypes.Structure):
-    """jne_sink: a write callback and its user pointer."""
+SINK_WRITE_RECORDS = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int64,
+                                      ctypes.c_int, ctypes.POINTER(ctypes.c_ubyte), ctypes.c_int64, ctypes.c_int)
 
-    _fields_ = [("write", SINK_WRITE), ("user", ctypes.c_void_p)]
+
+class Sink(ctypes.Structure):
+    """jne_sink: a write callback, its user pointer, and the optional callback
+    that takes records packed on the GPU instead of eigenvalues."""
+
+    _fields_ = [("write", SINK_WRITE), ("user", ctypes.c_void_p), ("write_records", SINK_WRITE_RECORDS)]
 
 
 class Completion(ctypes.Structure):
@@ -201,6 +207,10 @@ def lib() -> ctypes.CDLL:
         u32p, i64p, ip = ctypes.POINTER(c_u32), ctypes.POINTER(c_i64), ctypes.POINTER(c_int)
         L.jne_dat_open.argtypes = [ctypes.c_char_p, c_int, c_int, c_u32, ctypes.POINTER(vp), i64p]
         L.jne_dat_append.argtypes = [vp, u32p, dp, c_i64, c_int]
+        L.jne_dat_append_packed.argtypes = [vp, c_u32, c_i64, c_int, vp]
+        L.jne_record_bytes.argtypes = [c_u32, c_i64, c_int]
+        L.jne_record_bytes.restype = c_i64
+        L.jne_pack_records_device.argtypes = [vp, c_u32, c_i64, c_int, vp, vp, c_i64, vp]
         L.jne_dat_finish.argtypes = [vp]
         L.jne_dat_abandon.argtypes = [vp]
         L.jne_dat_abandon.restype = None
@@ -303,6 +313,15 @@ class Engine:
                                                     ctypes.c_void_p(stream)))
         return out.tolist()
 
+    def pack_records_device(self, seed_first: int, n: int, k: int, eigs_ptr: int, out_ptr: int, cap: int,
+                            stream: int = 0) -> int:
+        """jne_pack_records_device: the .dat records of n results (n x k doubles at device address eigs_ptr) of
+        seeds seed_first.. packed on the GPU into the 16-byte aligned device buffer at out_ptr (cap bytes);
+        asynchronous on `stream`.  Returns the byte count."""
+        self._check(self._L.jne_pack_records_device(self._h, seed_first, int(n), int(k), ctypes.c_void_p(eigs_ptr),
+                                                     ctypes.c_void_p(out_ptr), int(cap), ctypes.c_void_p(stream)))
+        return record_bytes(seed_first, n, k)
+
     def probe_rates(self) -> Dict[str, float]:
         """Measured pipe rates of this GPU: normals/s of the kernels' RNG code, and
         FP64-FMA, TF32-mma, FP32-FMA and FP16-mma flop/s."""
@@ -382,11 +401,15 @@ class Engine:
         sink = Sink(SINK_WRITE(cb), None)
         self._check(self._L.jne_run_batch_sink(self._h, arr, len(reqs), ctypes.byref(sink)))
 
-    def run_batch_to_dat(self, reqs: Sequence[dict], data_dir: str, finish: bool = True) -> None:
-        """The batch streamed by jne_dat_sink into each request's simulation file under data_dir."""
+    def run_batch_to_dat(self, reqs: Sequence[dict], data_dir: str, finish: bool = True,
+                         device_pack: bool = True) -> None:
+        """The batch streamed by jne_dat_sink into each request's simulation file under data_dir, with the
+        records packed on the GPU (device_pack) or encoded on the host: the same bytes."""
         arr = self._requests(reqs)
         sink = Sink()
         _dat_check(self._L.jne_dat_sink_open(os.fsencode(data_dir), arr, len(reqs), ctypes.byref(sink)))
+        if not device_pack:
+            sink.write_records = SINK_WRITE_RECORDS()
         rc = self._L.jne_run_batch_sink(self._h, arr, len(reqs), ctypes.byref(sink))
         rc2 = self._L.jne_dat_sink_close(ctypes.byref(sink), int(finish and rc == JNE_OK))
         self._check(rc)
@@ -537,6 +560,13 @@ class DatWriter:
         _dat_check(lib().jne_dat_append(self._h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _dp(e),
                                         len(s), e.shape[1]))
 
+    def append_packed(self, seed_first: int, n: int, k: int, records: bytes) -> None:
+        """jne_dat_append_packed: n records of seeds seed_first.. already packed (record_bytes(...) bytes)."""
+        if len(records) != record_bytes(seed_first, n, k):
+            raise ValueError("records must hold record_bytes(seed_first, n, k) bytes")
+        buf = ctypes.create_string_buffer(bytes(records), len(records))
+        _dat_check(lib().jne_dat_append_packed(self._h, seed_first, int(n), int(k), buf))
+
     def append_eigenvalues(self, seed: int, eigenvalues: Sequence[float]) -> None:
         self.append([seed], np.asarray(eigenvalues, dtype=np.float64).reshape(1, -1))
 
@@ -548,6 +578,11 @@ class DatWriter:
         """Close without the EOF trailer (as an interrupted run leaves the file)."""
         h, self._h = self._h, None
         lib().jne_dat_abandon(h)
+
+
+def record_bytes(seed_first: int, n: int, k: int) -> int:
+    """jne_record_bytes: bytes of the .dat records of n consecutive seeds with k values each (-1: bad arguments)."""
+    return int(lib().jne_record_bytes(seed_first, int(n), int(k)))
 
 
 def read_dat(path: str) -> Tuple[Records, int, int, int]:

@@ -79,6 +79,8 @@ void jne_close(jne_context* c) {
     cudaFree(c->d_sink_st[i]);
     cudaFreeHost(c->h_sink[i]);
     cudaFreeHost(c->h_sink_st[i]);
+    cudaFree(c->d_pack[i]);
+    cudaFreeHost(c->h_pack[i]);
     if (c->ev_sink[i]) cudaEventDestroy(c->ev_sink[i]);
     cudaFree(c->d_reqs[i]);
     cudaFree(c->d_rtab[i]);

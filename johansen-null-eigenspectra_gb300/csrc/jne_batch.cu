@@ -262,11 +262,13 @@ int jne_run_batch_status(jne_context* c, const jne_request* reqs, int n_req, dou
 namespace {
 
 // One round of a streamed batch in flight: its parts (request, first seed,
-// runs, offset of its results in the slot's buffers).
+// runs, offset of its results in the slot's buffers; with packed records, the
+// offset and length of their bytes).
 struct SinkPart {
   int req;
   uint32_t seed_first;
   int64_t n, off;
+  int64_t boff, nbytes;
 };
 struct SinkRound {
   std::vector<SinkPart> parts;
@@ -284,7 +286,10 @@ int deliver(jne_context* c, const jne_request* reqs, const jne_sink* sink, int s
     const int st = status_code(c->h_sink_st[s][p]);
     if (st != JNE_OK && *worst == JNE_OK) *worst = st;
     const int k = jne_eigen_count(reqs[q.req].model, reqs[q.req].dim);
-    const int rc = sink->write(sink->user, q.req, q.seed_first, q.n, k, c->h_sink[s] + q.off, st);
+    const int rc = sink->write_records
+                       ? sink->write_records(sink->user, q.req, q.seed_first, q.n, k, c->h_pack[s] + q.boff,
+                                             q.nbytes, st)
+                       : sink->write(sink->user, q.req, q.seed_first, q.n, k, c->h_sink[s] + q.off, st);
     if (rc) return fail(c, rc, "the sink stopped the batch");
   }
   return JNE_OK;
@@ -294,7 +299,9 @@ int deliver(jne_context* c, const jne_request* reqs, const jne_sink* sink, int s
 
 int jne_run_batch_sink(jne_context* c, const jne_request* reqs, int n_req, const jne_sink* sink) {
   if (!c) return JNE_ERR_ARG;
-  if (!sink || !sink->write || n_req < 0 || (n_req > 0 && !reqs)) return fail(c, JNE_ERR_ARG, "null sink or requests");
+  if (!sink || (!sink->write && !sink->write_records) || n_req < 0 || (n_req > 0 && !reqs))
+    return fail(c, JNE_ERR_ARG, "null sink or requests");
+  const bool packed = sink->write_records != nullptr;  // records packed on the GPU
   int rc;
   for (int i = 0; i < n_req; i++) {
     if ((rc = check_common(c, reqs[i].model, reqs[i].dim, reqs[i].steps, reqs[i].n_runs, reqs[i].precision)))
@@ -324,22 +331,28 @@ int jne_run_batch_sink(jne_context* c, const jne_request* reqs, int n_req, const
     SinkRound& rd = rounds[s];
     rd.parts.clear();
     std::vector<jne_request> sub;
-    int64_t doubles = 0;
+    int64_t doubles = 0, bytes = 0;
     for (int i : act) {
       const int64_t n = std::min<int64_t>(share, reqs[i].n_runs - next[(size_t)i]);
       jne_request r = reqs[i];
       r.seed_first = reqs[i].seed_first + (uint32_t)next[(size_t)i];
       r.n_runs = n;
       sub.push_back(r);
-      rd.parts.push_back({i, r.seed_first, n, doubles});
-      doubles += n * jne_eigen_count(r.model, r.dim);
+      const int k = jne_eigen_count(r.model, r.dim);
+      const int64_t nb = packed ? jne_record_bytes(r.seed_first, n, k) : 0;
+      rd.parts.push_back({i, r.seed_first, n, doubles, bytes, nb});
+      doubles += n * k;
+      bytes += (nb + 15) / 16 * 16;  // every part's records start 16-byte aligned
       next[(size_t)i] += n;
     }
     const size_t np = rd.parts.size();
     if ((rc = ensure(c, &c->d_sink[s], &c->d_sink_cap[s], (size_t)doubles, "sink results")) ||
         (rc = ensure(c, &c->d_sink_st[s], &c->d_sink_st_cap[s], np, "sink status words")) ||
-        (rc = ensure_pinned(c, &c->h_sink[s], &c->h_sink_cap[s], (size_t)doubles)) ||
         (rc = ensure_pinned(c, &c->h_sink_st[s], &c->h_sink_st_cap[s], np)))
+      break;
+    if (packed ? ((rc = ensure(c, &c->d_pack[s], &c->d_pack_cap[s], (size_t)bytes, "sink records")) ||
+                  (rc = ensure_pinned(c, &c->h_pack[s], &c->h_pack_cap[s], (size_t)bytes)))
+               : (rc = ensure_pinned(c, &c->h_sink[s], &c->h_sink_cap[s], (size_t)doubles)))
       break;
     std::vector<double*> outs(np);
     std::vector<unsigned int*> words(np);
@@ -353,8 +366,20 @@ int jne_run_batch_sink(jne_context* c, const jne_request* reqs, int n_req, const
       break;
     }
     if ((rc = run_batch(c, sub.data(), (int)np, outs.data(), st, words.data()))) break;
-    if ((e = cudaMemcpyAsync(c->h_sink[s], c->d_sink[s], sizeof(double) * doubles, cudaMemcpyDeviceToHost, st)) !=
-            cudaSuccess ||
+    if (packed) {  // each part's records, packed where its results lie
+      for (size_t p = 0; p < np && e == cudaSuccess; p++) {
+        const SinkPart& q = rd.parts[p];
+        e = jne_launch_pack_records(c->d_sink[s] + q.off, c->d_pack[s] + q.boff, q.seed_first, q.n,
+                                    jne_eigen_count(sub[p].model, sub[p].dim), c->sms, st);
+      }
+      if (e != cudaSuccess) {
+        rc = cuda_fail(c, e, "sink record packer");
+        break;
+      }
+    }
+    if ((e = packed ? cudaMemcpyAsync(c->h_pack[s], c->d_pack[s], (size_t)bytes, cudaMemcpyDeviceToHost, st)
+                    : cudaMemcpyAsync(c->h_sink[s], c->d_sink[s], sizeof(double) * doubles, cudaMemcpyDeviceToHost,
+                                      st)) != cudaSuccess ||
         (e = cudaMemcpyAsync(c->h_sink_st[s], c->d_sink_st[s], sizeof(unsigned int) * np, cudaMemcpyDeviceToHost,
                              st)) != cudaSuccess ||
         (e = cudaEventRecord(c->ev_sink[s], st)) != cudaSuccess) {

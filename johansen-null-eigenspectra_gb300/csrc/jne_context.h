@@ -83,6 +83,11 @@ struct jne_context {
   size_t h_sink_cap[2] = {0, 0};
   unsigned int* h_sink_st[2] = {nullptr, nullptr};
   size_t h_sink_st_cap[2] = {0, 0};
+  // ... and, for sinks that take packed records, the records on the device and their pinned host copy
+  unsigned char* d_pack[2] = {nullptr, nullptr};
+  size_t d_pack_cap[2] = {0, 0};
+  unsigned char* h_pack[2] = {nullptr, nullptr};
+  size_t h_pack_cap[2] = {0, 0};
   cudaEvent_t ev_sink[2] = {nullptr, nullptr};
   // per-kernel event timing (jne_profile)
   bool profiling = false;

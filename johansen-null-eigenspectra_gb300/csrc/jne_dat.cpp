@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/jne.h"
+#include "jne_records.h"
 
 namespace {
 
@@ -201,8 +202,17 @@ void decode_values(const std::vector<unsigned char>& b, const Parsed& p, double*
   const size_t hw = std::max(1u, std::thread::hardware_concurrency());
   const size_t nt = std::min<size_t>(std::min<size_t>(hw, 16), n / 65536 + 1);
   std::vector<std::thread> pool;
-  for (size_t t = 1; t < nt; t++) pool.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+  size_t started = 0;  // a part whose thread cannot be started is decoded here (no exception leaves the C ABI)
+  for (size_t t = 1; t < nt; t++) {
+    try {
+      pool.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+      started = t;
+    } catch (const std::system_error&) {
+      break;
+    }
+  }
   work(0, n / nt);
+  for (size_t t = started + 1; t < nt; t++) work(n * t / nt, n * (t + 1) / nt);
   for (auto& th : pool) th.join();
 }
 
@@ -239,6 +249,59 @@ struct jne_dat_writer {
   std::vector<char> buf;
   std::vector<unsigned char> rec;
 };
+
+namespace {
+
+// The eigenvalue count of a record: at most 255 (u8), the same for every
+// record of a file (the first one written sets it).
+int check_count(jne_dat_writer* w, int k) {
+  if (k > 255)
+    return dat_fail(JNE_ERR_FORMAT, "Too many eigenvalues: " + std::to_string(k) + " exceeds maximum of 255");
+  if (k < 0) return dat_fail(JNE_ERR_ARG, "negative eigenvalue count");
+  if (w->per_run < 0) w->per_run = k;
+  if (k != w->per_run)
+    return dat_fail(JNE_ERR_FORMAT, "Eigenvalue count mismatch: expected " + std::to_string(w->per_run) +
+                                        ", actual " + std::to_string(k) + " (model " + std::to_string(w->model) +
+                                        ", dim " + std::to_string(w->dim) + ", steps " + std::to_string(w->steps) +
+                                        ")");
+  return JNE_OK;
+}
+
+// Writes a block of n whole records straight to the file descriptor (after
+// what stdio holds), so a short write is seen here with its exact length, not
+// later at close.  On a short write the file and the count stay in step:
+// whole(wrote, &bytes) gives the whole records among the bytes written and
+// their length, the file is cut back to their end (never a partial record),
+// and they are counted.
+template <typename Whole>
+int write_block(jne_dat_writer* w, const unsigned char* p, size_t size, int64_t n, Whole&& whole) {
+  if (std::fflush(w->f) != 0) return dat_fail(JNE_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+  const int fd = fileno(w->f);
+  const off_t start = lseek(fd, 0, SEEK_CUR);
+  size_t wrote = 0;
+  int err = 0;
+  while (wrote < size) {
+    const ssize_t r = ::write(fd, p + wrote, size - wrote);
+    if (r < 0 && errno == EINTR) continue;
+    if (r <= 0) {
+      err = r < 0 ? errno : EIO;
+      break;
+    }
+    wrote += (size_t)r;
+  }
+  if (wrote != size) {
+    size_t bytes = 0;
+    const int64_t done = whole(wrote, &bytes);
+    if (start >= 0 && ftruncate(fd, start + (off_t)bytes) == 0) lseek(fd, start + (off_t)bytes, SEEK_SET);
+    w->count += done;
+    return dat_fail(JNE_ERR_IO, "record write failed after " + std::to_string(w->count) + " records: " +
+                                    std::strerror(err));
+  }
+  w->count += n;
+  return JNE_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -311,23 +374,14 @@ int jne_dat_open(const char* path, int model, int dim, uint32_t steps, jne_dat_w
 
 int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs, int64_t n, int k) {
   if (!w || (n > 0 && (!seeds || !eigs)) || n < 0) return dat_fail(JNE_ERR_ARG, "null argument");
-  if (k > 255)
-    return dat_fail(JNE_ERR_FORMAT, "Too many eigenvalues: " + std::to_string(k) + " exceeds maximum of 255");
-  if (k < 0) return dat_fail(JNE_ERR_ARG, "negative eigenvalue count");
-  if (n == 0) return JNE_OK;
-  if (w->per_run < 0) w->per_run = k;
-  if (k != w->per_run)
-    return dat_fail(JNE_ERR_FORMAT, "Eigenvalue count mismatch: expected " + std::to_string(w->per_run) +
-                                        ", actual " + std::to_string(k) + " (model " + std::to_string(w->model) +
-                                        ", dim " + std::to_string(w->dim) + ", steps " + std::to_string(w->steps) +
-                                        ")");
+  if (n == 0) return k < 0 || k > 255 ? check_count(w, k) : JNE_OK;
+  const int crc = check_count(w, k);
+  if (crc) return crc;
   // Records are encoded into one block and written with one call per block;
   // large batches are encoded by several threads, each into its own byte
   // range (record sizes differ only in the seed's ULEB128 length).
   const size_t fixed = 1 + 8 * (size_t)k;
-  auto rec_size = [&](uint32_t seed) {
-    return fixed + 1 + (seed >= (1u << 7)) + (seed >= (1u << 14)) + (seed >= (1u << 21)) + (seed >= (1u << 28));
-  };
+  auto rec_size = [&](uint32_t seed) { return fixed + (size_t)jne_uleb_len(seed); };
   auto encode = [&](int64_t r0, int64_t r1, unsigned char* out) {
     for (int64_t r = r0; r < r1; r++) {
       size_t len = uleb_encode(seeds[r], out);
@@ -363,40 +417,32 @@ int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs,
     encode(part_lo(0), part_lo(1), w->rec.data());
     for (int p = started + 1; p < parts; p++) encode(part_lo(p), part_lo(p + 1), w->rec.data() + off[(size_t)p]);
     for (std::thread& t : th) t.join();
-    // The block goes straight to the file descriptor (after what stdio holds),
-    // so a short write is seen here with its exact length, not later at close.
-    if (std::fflush(w->f) != 0) return dat_fail(JNE_ERR_IO, std::string("write failed: ") + std::strerror(errno));
-    const int fd = fileno(w->f);
-    const off_t start = lseek(fd, 0, SEEK_CUR);
-    size_t wrote = 0;
-    int err = 0;
-    while (wrote < w->rec.size()) {
-      const ssize_t r = ::write(fd, w->rec.data() + wrote, w->rec.size() - wrote);
-      if (r < 0 && errno == EINTR) continue;
-      if (r <= 0) {
-        err = r < 0 ? errno : EIO;
-        break;
-      }
-      wrote += (size_t)r;
-    }
-    if (wrote != w->rec.size()) {
-      // Keep the file and the count in step: count the whole records the
-      // short write holds and cut the file back to their end, so the file
-      // never ends in a partial record.
+    const int rc = write_block(w, w->rec.data(), w->rec.size(), b1 - b0, [&](size_t wrote, size_t* bytes) {
       int64_t whole = 0;
-      size_t bytes = 0;
-      for (int64_t r = b0; r < b1 && bytes + rec_size(seeds[r]) <= wrote; r++) {
-        bytes += rec_size(seeds[r]);
+      for (int64_t r = b0; r < b1 && *bytes + rec_size(seeds[r]) <= wrote; r++) {
+        *bytes += rec_size(seeds[r]);
         whole++;
       }
-      if (start >= 0 && ftruncate(fd, start + (off_t)bytes) == 0) lseek(fd, start + (off_t)bytes, SEEK_SET);
-      w->count += whole;
-      return dat_fail(JNE_ERR_IO, "record write failed after " + std::to_string(w->count) + " records: " +
-                                      std::strerror(err));
-    }
-    w->count += b1 - b0;
+      return whole;
+    });
+    if (rc) return rc;
   }
   return JNE_OK;
+}
+
+int jne_dat_append_packed(jne_dat_writer* w, uint32_t seed_first, int64_t n, int k, const unsigned char* records) {
+  if (!w || n < 0 || (n > 0 && !records)) return dat_fail(JNE_ERR_ARG, "null argument");
+  int rc = check_count(w, k);
+  if (rc) return rc;
+  if ((uint64_t)seed_first + (uint64_t)n > 0x100000000ull) return dat_fail(JNE_ERR_ARG, "seed range exceeds u32");
+  if (n == 0) return JNE_OK;
+  const jne_record_bands bands = jne_make_bands(seed_first, n, k);
+  return write_block(w, records, (size_t)jne_records_bytes(seed_first, n, k), n, [&](size_t wrote, size_t* bytes) {
+    long long start = 0;
+    const long long r = wrote == 0 ? 0 : jne_record_at(bands, k, (long long)wrote, &start);
+    *bytes = (size_t)start;
+    return (int64_t)r;
+  });
 }
 
 int jne_dat_finish(jne_dat_writer* w) {
@@ -459,6 +505,14 @@ int dat_sink_write(void* user, int req, uint32_t seed_first, int64_t n, int k, c
   return jne_dat_append(d->of_req[(size_t)req], d->seeds.data(), eigs, n, k);
 }
 
+// the same records, packed on the GPU
+int dat_sink_write_records(void* user, int req, uint32_t seed_first, int64_t n, int k, const unsigned char* records,
+                           int64_t, int status) {
+  DatSink* d = static_cast<DatSink*>(user);
+  if (status != JNE_OK) return status;
+  return jne_dat_append_packed(d->of_req[(size_t)req], seed_first, n, k, records);
+}
+
 }  // namespace
 
 extern "C" {
@@ -467,6 +521,7 @@ int jne_dat_sink_open(const char* data_dir, const jne_request* reqs, int n_req, 
   if (!out || n_req < 0 || (n_req > 0 && !reqs)) return dat_fail(JNE_ERR_ARG, "null argument");
   out->write = nullptr;
   out->user = nullptr;
+  out->write_records = nullptr;
   const std::string dir = data_dir && *data_dir ? data_dir : "data";
   int rc = mkdirs(dir);
   if (rc) return rc;
@@ -497,6 +552,7 @@ int jne_dat_sink_open(const char* data_dir, const jne_request* reqs, int n_req, 
     return rc;
   }
   out->write = dat_sink_write;
+  out->write_records = dat_sink_write_records;
   out->user = d;
   return JNE_OK;
 }
@@ -516,6 +572,7 @@ int jne_dat_sink_close(jne_sink* sink, int finish) {
   delete d;
   sink->user = nullptr;
   sink->write = nullptr;
+  sink->write_records = nullptr;
   return rc;
 }
 

@@ -51,5 +51,9 @@ cudaError_t jne_launch_accum_mixed_b6(const jne_accum_args& a, const jne_finaliz
 cudaError_t jne_launch_accum_mixed_ext(const jne_accum_args& a, const jne_finalize_args* fin, int sms,
                                        cudaStream_t st);
 cudaError_t jne_launch_finalize(const jne_finalize_args& f, int sms, cudaStream_t st);
+// The .dat records of n results of consecutive seeds (jne_pack.cu): out is
+// 16-byte aligned and holds jne_records_bytes(seed_first, n, k) bytes.
+cudaError_t jne_launch_pack_records(const double* eigs, unsigned char* out, uint32_t seed_first, long long n, int k,
+                                    int sms, cudaStream_t st);
 cudaError_t jne_launch_export(int dim, int steps, int n_runs, uint32_t seed_first, uint32_t key0, uint32_t key1,
                               double scale, double* out, uint32_t* words, cudaStream_t st);

@@ -261,3 +261,90 @@ def test_dat_sink_host_side(jne, tmp):
     recs, model, dim, steps = jne.read_dat(os.path.join(tmp, "eigenvalues_model3_dim2_steps50.dat"))
     assert list(recs.seeds) == [1, 2, 3] and np.array_equal(recs.eigs, b)
     assert open(os.path.join(tmp, "eigenvalues_model3_dim2_steps50.dat"), "rb").read()[-17:-9] == b"EOF_MARK"
+
+
+def _record_part(oracle, seed_first, eigs):
+    """The records of seeds seed_first.. in the oracle's restatement of the format (no header, no trailer)."""
+    recs = [(seed_first + r, list(eigs[r])) for r in range(eigs.shape[0])]
+    return oracle.dat_bytes(0, 2, 100, recs, finished=False)[18:]
+
+
+def test_record_bytes_closed_form(jne, oracle):
+    """jne_record_bytes against the ULEB128 lengths of the restatement, across every length threshold."""
+    for a in (0, 1, 126, 127, 128, 16383, 16384, 2**21 - 2, 2**28 - 1, 2**32 - 3):
+        for n in (0, 1, 2, 5, 300):
+            if a + n > 2**32:
+                continue
+            for k in (1, 2, 13, 255):
+                want = sum(len(oracle.uleb128_encode(a + r)) + 1 + 8 * k for r in range(n))
+                assert jne.record_bytes(a, n, k) == want, (a, n, k)
+    assert jne.record_bytes(2**32 - 1, 1, 3) == 5 + 1 + 24
+    for bad in ((2**32 - 1, 2, 3), (0, -1, 3), (0, 1, 256), (0, 1, -1)):
+        assert jne.record_bytes(*bad) == -1
+
+
+def test_append_packed_matches_format_restatement(jne, oracle, tmp):
+    """Packed records appended as they are give the file jne_dat_append gives (the restatement's bytes),
+    with the same count checks."""
+    rng = np.random.default_rng(5)
+    eigs = rng.standard_normal((400, 2))
+    a = 16200  # the seeds cross the 2- to 3-byte ULEB128 boundary at 16384
+    recs = _record_part(oracle, a, eigs)
+    split = jne.record_bytes(a, 150, 2)
+    path = os.path.join(tmp, "p.dat")
+    w = jne.DatWriter(path, 0, 2, 100)
+    w.append_packed(a, 150, 2, recs[:split])
+    w.append_packed(a + 150, 250, 2, recs[split:])
+    w.append_packed(a + 400, 0, 2, b"")
+    w.finish()
+    assert open(path, "rb").read() == oracle.dat_bytes(0, 2, 100, [(a + r, list(eigs[r])) for r in range(400)])
+    w = jne.DatWriter(path, 0, 2, 100)
+    with pytest.raises(jne.DatError) as ei:  # the file holds 2 values per record
+        w.append_packed(1, 1, 3, bytes(jne.record_bytes(1, 1, 3)))
+    assert ei.value.code == jne.JNE_ERR_FORMAT and "count mismatch" in str(ei.value)
+    with pytest.raises(ValueError):
+        w.append_packed(1, 2, 2, recs[:10])
+    w.abandon()
+
+
+_SHORT_PACKED_CHILD = r"""
+import os, resource, signal, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import __graft_entry__ as entry
+jne, oracle = entry.load_package(), entry.load_oracle()
+path, limit = sys.argv[2], int(sys.argv[3])
+n = 100_000
+eigs = np.arange(2 * n, dtype=float).reshape(n, 2)
+recs = oracle.dat_bytes(0, 2, 100, [(3 + r, list(eigs[r])) for r in range(n)], finished=False)[18:]
+w = jne.DatWriter(path, 0, 2, 100)
+w.append(range(1, 3), np.ones((2, 2)))
+signal.signal(signal.SIGXFSZ, signal.SIG_IGN)
+resource.setrlimit(resource.RLIMIT_FSIZE, (limit, limit))
+try:
+    w.append_packed(3, n, 2, recs)
+except jne.DatError as e:
+    print("IOERR", e.code)
+w.abandon()
+"""
+
+
+def test_short_packed_write_leaves_whole_records(jne, tmp):
+    """A packed append cut short by the file system also leaves the file at a record boundary."""
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+
+    path = os.path.join(tmp, "short_packed.dat")
+    limit = 100_003
+    out = subprocess.run([sys.executable, "-c", _SHORT_PACKED_CHILD, ROOT, path, str(limit)],
+                         capture_output=True, text=True, timeout=120)
+    assert f"IOERR {jne.JNE_ERR_IO}" in out.stdout, out.stdout + out.stderr
+    size = os.path.getsize(path)
+    assert size <= limit
+    recs, model, dim, steps = jne.read_dat(path)
+    n = len(recs.seeds)
+    assert n > 1000 and list(recs.seeds[:3]) == [1, 2, 3]
+    assert np.array_equal(recs.eigs[2:], np.arange(2 * (n - 2), dtype=float).reshape(n - 2, 2))
+    assert size == 18 + jne.record_bytes(1, n, 2)
