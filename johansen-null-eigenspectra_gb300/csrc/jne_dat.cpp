@@ -432,10 +432,10 @@ int jne_dat_append(jne_dat_writer* w, const uint32_t* seeds, const double* eigs,
 
 int jne_dat_append_packed(jne_dat_writer* w, uint32_t seed_first, int64_t n, int k, const unsigned char* records) {
   if (!w || n < 0 || (n > 0 && !records)) return dat_fail(JNE_ERR_ARG, "null argument");
-  int rc = check_count(w, k);
-  if (rc) return rc;
   if ((uint64_t)seed_first + (uint64_t)n > 0x100000000ull) return dat_fail(JNE_ERR_ARG, "seed range exceeds u32");
-  if (n == 0) return JNE_OK;
+  if (n == 0) return k < 0 || k > 255 ? check_count(w, k) : JNE_OK;  // as jne_dat_append
+  const int rc = check_count(w, k);
+  if (rc) return rc;
   const jne_record_bands bands = jne_make_bands(seed_first, n, k);
   return write_block(w, records, (size_t)jne_records_bytes(seed_first, n, k), n, [&](size_t wrote, size_t* bytes) {
     long long start = 0;
