@@ -690,11 +690,16 @@ int run_models(jne_context* ctx, const std::vector<int>& models, const std::vect
       abandon();
       return rc;
     }
-    writer = std::thread([&, buf = cur, i0 = i, n]() {
+    auto write_batch = [&, buf = cur, i0 = i, n]() {
       for (size_t m = 0; m < nm && !wrc; m++)
         if ((wrc = jne_dat_append(w[m], &remaining[i0], eig[buf][m].data(), n, jne_eigen_count(models[m], dim))))
           werr = g_err;
-    });
+    };
+    try {
+      writer = std::thread(write_batch);
+    } catch (const std::system_error&) {  // the thread cannot be started: write this batch here
+      write_batch();
+    }
     cur ^= 1;
     i = j;
   }

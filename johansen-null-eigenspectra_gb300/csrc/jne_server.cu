@@ -18,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -280,8 +281,13 @@ int jne_server_open(jne_context* c, const char* data_dir, long long iter_work, j
       delete s;
       return fail(c, JNE_ERR_CUDA, "server events");
     }
-  s->worker = std::thread(worker_loop, s);
-  if (!s->data_dir.empty()) s->writer = std::thread(writer_loop, s);
+  try {
+    s->worker = std::thread(worker_loop, s);
+    if (!s->data_dir.empty()) s->writer = std::thread(writer_loop, s);
+  } catch (const std::system_error&) {  // no exception leaves the C ABI
+    jne_server_close(s);                 // stops whichever thread started
+    return fail(c, JNE_ERR_IO, "cannot start the server's threads");
+  }
   *out = s;
   return JNE_OK;
 }
@@ -350,7 +356,7 @@ int jne_server_close(jne_server* s) {
     s->stopping = true;
     s->cv.notify_all();
   }
-  s->worker.join();
+  if (s->worker.joinable()) s->worker.join();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->writer_stop = true;
