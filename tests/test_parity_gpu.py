@@ -274,3 +274,26 @@ def test_seeds_at_the_top_of_the_u32_range(engine, oracle):
         ref = oracle.c_eigs_from_increments(model, dB)
         assert normwise_err(engine.eigs_seeded(model, dim, steps, first, n, precision=0), ref) < TOL_FP64
         assert normwise_err(engine.eigs_seeded(model, dim, steps, first, n, precision=1), ref, 1.0) < TOL_MIXED
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_distribution_vs_independent_stream_dim6(engine, oracle, precision):
+    """A middle shape (dim 6, T 5000, models 0-4): 4,000 GPU runs against 4,000 oracle runs of the independent
+    xoshiro256++ stream with untruncated normals -- two-sample KS on the trace and the largest eigenvalue, and
+    the 1/5/10/50/90/95/99 % quantiles within five Monte Carlo standard errors in rank space."""
+    import os
+
+    from scipy.stats import ks_2samp
+
+    n, dim, steps = 4000, 6, 5000
+    threads = max(1, min(32, os.cpu_count() or 1))
+    for model in range(5):
+        gpu = engine.eigs_seeded(model, dim, steps, 1, n, precision=precision)
+        cpu = oracle.c_eigs_seeded_xoshiro(model, dim, steps, 1, n, n_threads=threads, base_seed=0xD16)
+        assert np.all(np.isfinite(gpu))
+        for name, stat in (("trace", lambda e: e.sum(1)), ("maxeig", lambda e: e.max(1))):
+            a, b = np.sort(stat(gpu)), np.sort(stat(cpu))
+            assert ks_2samp(a, b).pvalue > 1e-4, (model, name)
+            for p in (0.01, 0.05, 0.1, 0.5, 0.9, 0.95, 0.99):
+                rank_b = np.searchsorted(b, oracle.percentile_value(a, p)) / n
+                assert abs(rank_b - p) < 5 * np.sqrt(2 * p * (1 - p) / n) + 2.0 / n, (model, name, p, rank_b)
